@@ -1,0 +1,166 @@
+"""Box-level checks of the CPU oracle: ghost fill, CFL, whole steps (CPU only).
+
+The ghost-fill and CFL cases restate rhyme_samr_bc_set_*_boundary_test.f90
+and rhyme_cfl_dt_test.f90; the whole-step cases check properties the
+reference's solve tests leave unpinned (conservation, symmetry, agreement of
+the two solver orderings, Sod against its analytic solution).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from refcheck import GAMMA, KB_AMU_SI, to_be
+
+from rhyme_gb300 import ic
+
+
+def _params(ndim, bc, limiter=2, solver_type=2, gamma=GAMMA["monatomic"]):
+    return dict(ndim=ndim, gamma=gamma, kb_amu=KB_AMU_SI, courant=0.8, limiter=limiter,
+                omega=0.0, vac_rho=0.0, vac_p=0.0, tol=1e-6, n_iter=100, bc=list(bc),
+                solver_type=solver_type)
+
+
+def _random_box(ndim, dims, seed=1):
+    rng = np.random.default_rng(seed)
+    shape = (ndim + 2,) + tuple(d + 4 for d in dims[::-1])
+    cells = np.zeros(shape)
+    interior = (slice(None),) + tuple(slice(2, d + 2) for d in dims[::-1])
+    rho = rng.uniform(0.5, 2.0, shape[1:])
+    vel = rng.uniform(-0.5, 0.5, (ndim,) + shape[1:])
+    p = rng.uniform(0.5, 2.0, shape[1:])
+    full = np.zeros(shape)
+    full[0] = rho
+    full[1:ndim + 1] = rho * vel
+    full[ndim + 1] = 0.5 * rho * (vel * vel).sum(0) + p / (GAMMA["monatomic"] - 1.0)
+    cells[interior] = full[interior]
+    return cells
+
+
+def _face(cells, ndim, axis, idx):
+    """Slice of ghost/interior layer `idx` (Fortran index) along `axis`,
+    restricted to interior transverse positions."""
+    sl = [slice(None)]
+    for a in range(ndim - 1, -1, -1):
+        if a == axis:
+            sl.append(idx + 1)
+        else:
+            sl.append(slice(2, cells.shape[1 + (ndim - 1 - a)] - 2))
+    return cells[tuple(sl)]
+
+
+@pytest.mark.parametrize("ndim,dims", [(1, [16]), (2, [16, 8]), (3, [16, 8, 4])])
+@pytest.mark.parametrize("bctype", [1, 2, 3])
+def test_set_boundaries(ndim, dims, bctype):
+    """rhyme_samr_bc_set_{left,right,...}_boundary_test.f90: exact copies,
+    negated normal momentum for reflective, wrap for periodic; corners kept."""
+    cells = _random_box(ndim, dims)
+    before = cells.copy()
+    oracle.set_boundaries(_params(ndim, [bctype] * 6), cells)
+    for axis in range(ndim):
+        N = dims[axis]
+        for ghost, src_refl, src_per in ((0, 1, N), (-1, 2, N - 1), (N + 1, N, 1), (N + 2, N - 1, 2)):
+            g = _face(cells, ndim, axis, ghost)
+            src = _face(cells, ndim, axis, src_per if bctype == 3 else src_refl)
+            exp = src.copy()
+            if bctype == 1:
+                exp[1 + axis] = -exp[1 + axis]
+            assert to_be(g, exp) or np.array_equal(g, exp)
+    # corners (ghost in two axes) untouched
+    if ndim >= 2:
+        assert np.array_equal(cells[:, 0, 0], before[:, 0, 0])
+        assert np.array_equal(cells[:, 1, 1], before[:, 1, 1])
+
+
+@pytest.mark.parametrize("ndim,dims", [(1, [32]), (2, [16, 8]), (3, [8, 8, 4])])
+def test_cfl_time_step(ndim, dims):
+    """rhyme_cfl_dt_test.f90:58-73: dt = c*min(dx)/max(|v|+cs)."""
+    cells = _random_box(ndim, dims)
+    dx = [1.0 / d for d in dims]
+    p = _params(ndim, [2] * 6)
+    dt = oracle.cfl_time_step(p, cells, dx)
+    interior = (slice(None),) + tuple(slice(2, d + 2) for d in dims[::-1])
+    u = cells[interior].reshape(ndim + 2, -1).T
+    _, _, cs = oracle.eos(ndim, p["gamma"], KB_AMU_SI, u, 0)
+    s = np.zeros(u.shape[0])
+    for a in range(ndim):
+        s = s + u[:, 1 + a] * u[:, 1 + a]
+    v = np.sqrt(s) / u[:, 0] + cs
+    exp = 0.8 * min(dx) / v.max()
+    assert to_be(dt, exp)
+
+
+def test_uniform_state_is_steady():
+    cells = np.zeros((5, 12, 12, 12))
+    cells[0] = 1.0
+    cells[1] = 0.3
+    cells[4] = 3.0
+    interior = (slice(None), slice(2, 10), slice(2, 10), slice(2, 10))
+    ref = cells[interior].copy()
+    oracle.run(_params(3, [3] * 6), cells, [1 / 8] * 3, 5)
+    assert np.allclose(cells[interior], ref, rtol=1e-14, atol=1e-14)
+
+
+@pytest.mark.parametrize("limiter", [1, 2, 3, 4])
+def test_periodic_conservation(limiter):
+    p = _params(2, [3] * 4 + [2, 2], limiter=limiter)
+    cells, dx, _ = ic.slab_2d(n=32, seed=3)
+    interior = (slice(None), slice(2, 34), slice(2, 34))
+    tot0 = cells[interior].sum(axis=(1, 2))
+    oracle.run(p, cells, dx, 20)
+    tot1 = cells[interior].sum(axis=(1, 2))
+    assert np.allclose(tot1, tot0, rtol=1e-13, atol=1e-13)
+
+
+def test_solver_orderings_agree():
+    """memory_intensive vs cpu_intensive differ only in rounding order."""
+    a, dx, _ = ic.slab_2d(n=32, seed=5)
+    b = a.copy()
+    oracle.run(_params(2, [3] * 4 + [2, 2], solver_type=2), a, dx, 10)
+    oracle.run(_params(2, [3] * 4 + [2, 2], solver_type=1), b, dx, 10)
+    assert np.allclose(a, b, rtol=1e-12, atol=1e-13)
+
+
+def test_1d_embedded_in_3d():
+    """A state varying along x only evolves identically in 1-D and 3-D."""
+    c1, dx, p1 = ic.riemann_1d(n=64, seed=7)
+    p1 = dict(p1)
+    c3 = np.zeros((5, 8, 8, 68))
+    c3[0] = c1[0]
+    c3[1] = c1[1]
+    c3[4] = c1[2]
+    c3[:, :2] = 0.0
+    c3[:, -2:] = 0.0
+    c3[:, :, :2] = 0.0
+    c3[:, :, -2:] = 0.0
+    p3 = dict(p1)
+    p3["ndim"] = 3
+    p3["bc"] = [2, 2, 3, 3, 3, 3]
+    oracle.run(p1, c1, [1 / 64], 20)
+    oracle.run(p3, c3, [1 / 64] * 3, 20)
+    for k in range(2, 6):
+        for j in range(2, 6):
+            assert np.allclose(c3[0, k, j, 2:-2], c1[0, 2:-2], rtol=1e-13, atol=1e-14)
+            assert np.allclose(c3[4, k, j, 2:-2], c1[2, 2:-2], rtol=1e-13, atol=1e-14)
+
+
+def test_sod_against_analytic(golden_dir):
+    """1-D Sod (gamma=1.4) evolved to t~0.2 matches the analytic density
+    profile to first-order accuracy near discontinuities (L1 < 1e-2)."""
+    import os
+    n = 500
+    g = GAMMA["diatomic"]
+    cells = np.zeros((3, n + 4))
+    x = -0.5 + (np.arange(n) + 0.5) / n
+    rho = np.where(x < 0, 1.0, 0.125)
+    pr = np.where(x < 0, 1.0, 0.1)
+    cells[0, 2:-2] = rho
+    cells[2, 2:-2] = pr / (g - 1.0)
+    p = _params(1, [2] * 6, limiter=1, gamma=g)
+    p["tol"], p["n_iter"] = 1e-8, 1000
+    t = 0.0
+    while t < 0.2:
+        dt = oracle.run(p, cells, [1.0 / n], 1)[0]
+        t += dt
+    ref = np.loadtxt(os.path.join(golden_dir, "sod_t0.2_analytical.csv"), delimiter=",", comments="#")
+    rho_ref = np.interp(x, ref[:, 0] * (t / 0.2), ref[:, 1])
+    assert np.mean(np.abs(cells[0, 2:-2] - rho_ref)) < 1e-2
