@@ -1,0 +1,197 @@
+/*
+ * rhyme_gpu.h -- C-ABI of the GB300 (sm_103a) MUSCL-Hancock hydro step for
+ * Rhyme SAMR boxes.
+ *
+ * The Fortran driver (src/main.f90) reaches these entry points through a thin
+ * ISO_C_BINDING shim that keeps Rhyme's module interfaces; each declaration
+ * names the reference interface it replaces (paths relative to Rhyme's src/).
+ *
+ * Conventions
+ *  - Every function returns 0 (RHYME_GPU_OK) or a negative RHYME_GPU_E* code;
+ *    rhyme_gpu_last_error() gives the message of the last failure on a
+ *    context. The reference has no error returns (it calls logger%err and
+ *    goes on, rhyme_muscl_hancock_solve.f90:24-26); the shim maps a non-zero
+ *    code to logger%err.
+ *  - A box's `cells` is the caller's Fortran array
+ *    cells(-1:N1+2, -1:N2+2, -1:N3+2, 1:NCMP) (rhyme_samr_init_box.f90:29-33),
+ *    column-major and contiguous, ghost width 2 on every active axis
+ *    (rhyme_initial_condition_init_simple.f90:31). The library mirrors the
+ *    hydro components 1..NDIM+2 (rho, rho*u[, rho*v[, rho*w]], e_tot;
+ *    rhyme_units.f90:32-36) on the device and never frees the host array.
+ *    Axes beyond NDIM have dims 1 and no ghosts.
+ *  - Between rhyme_gpu_sync_to_device and rhyme_gpu_sync_to_host the device
+ *    copy is authoritative.
+ *  - Axis arguments are 0-based (x = 0); the Fortran shim subtracts one.
+ *  - One context is used by one host thread at a time; it owns one CUDA
+ *    stream, on which every call below is ordered.
+ */
+#ifndef RHYME_GPU_H
+#define RHYME_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RHYME_GPU_ABI_VERSION 1
+
+enum {
+  RHYME_GPU_OK = 0,
+  RHYME_GPU_EINVAL = -1,     /* bad argument or unsupported parameter */
+  RHYME_GPU_ENOMEM = -2,     /* device or pinned allocation failed */
+  RHYME_GPU_ECUDA = -3,      /* a CUDA runtime call failed */
+  RHYME_GPU_ETIMEDOUT = -4,  /* a bounded host wait ran out */
+  RHYME_GPU_ENANSTATE = -5,  /* the state holds NaN/Inf or non-positive rho */
+  RHYME_GPU_ENOTFOUND = -6   /* unknown box handle */
+};
+
+/* Slope limiter ids: slid, rhyme_slope_limiter.f90:6-10. */
+enum { RHYME_GPU_VAN_LEER = 1, RHYME_GPU_MINMOD = 2, RHYME_GPU_VAN_ALBADA = 3,
+       RHYME_GPU_SUPERBEE = 4 };
+/* Boundary ids: bcid, rhyme_samr_bc.f90:9-12. */
+enum { RHYME_GPU_REFLECTIVE = 1, RHYME_GPU_OUTFLOW = 2, RHYME_GPU_PERIODIC = 3,
+       RHYME_GPU_INFLOW = 4 };
+/* Solver ids: mhid, rhyme_muscl_hancock.f90:10-15. */
+enum { RHYME_GPU_CPU_INTENSIVE = 1, RHYME_GPU_MEMORY_INTENSIVE = 2 };
+/* Arithmetic of the step (this library). */
+enum { RHYME_GPU_FP64 = 0, RHYME_GPU_MIXED = 1 };
+
+/*
+ * Run parameters: the values Rhyme's modules hold after load_params
+ * (rhyme_param_parser_load_params.f90: BCs :259-293, courant :307, gas :314,
+ * Riemann :493-499, limiter :512-513, solver :523) and rhyme_*_init.
+ */
+typedef struct rhyme_gpu_params {
+  int ndim;          /* NDIM (1, 2 or 3) */
+  int limiter;       /* sl%type */
+  int n_iteration;   /* rp%irs%n_iteration */
+  int solver_type;   /* mh%solver_type */
+  int bc[6];         /* bc%types(left, right, bottom, top, back, front) */
+  int precision;     /* RHYME_GPU_FP64 or RHYME_GPU_MIXED */
+  int reserved;      /* must be 0 */
+  double gamma;      /* get_gamma(), rhyme_thermo_base_get_gamma.f90:8-19 */
+  double kb_amu;     /* units%kb%v / units%amu%v, rhyme_thermo_base.f90:130 */
+  double courant;    /* cfl%courant_number */
+  double omega;      /* sl%w */
+  double vacuum_density;   /* rp%w_vacuum(cid%rho) */
+  double vacuum_pressure;  /* rp%w_vacuum(cid%p) */
+  double tolerance;        /* rp%irs%tolerance */
+  double inflow[6][5];     /* bc%cons_inflows(rho:e_tot, side) for inflow faces */
+} rhyme_gpu_params;
+
+typedef struct rhyme_gpu_ctx rhyme_gpu_ctx;
+
+/* ABI version of the loaded library (RHYME_GPU_ABI_VERSION). */
+int rhyme_gpu_abi_version(void);
+
+/*
+ * Creates a context on the current CUDA device with the run parameters.
+ * Replaces the module set-up of rhyme_riemann_problem_init
+ * (rhyme_riemann_problem.f90:64-69, rhyme_riemann_problem_init.f90:20-27),
+ * rhyme_irs_init (rhyme_irs_init.f90:21-27), rhyme_muscl_hancock_init
+ * (rhyme_muscl_hancock.f90:22-27), rhyme_cfl_init (rhyme_cfl.f90:12-17) and
+ * rhyme_samr_bc_init (rhyme_samr_bc.f90:31-36).
+ */
+int rhyme_gpu_create(rhyme_gpu_ctx** ctx, const rhyme_gpu_params* params);
+int rhyme_gpu_destroy(rhyme_gpu_ctx* ctx);
+
+/* Message of the last failure on ctx ("" if none). */
+const char* rhyme_gpu_last_error(const rhyme_gpu_ctx* ctx);
+
+/* The cudaStream_t (as void*) every call on ctx is ordered on. */
+int rhyme_gpu_get_stream(rhyme_gpu_ctx* ctx, void** stream);
+
+/*
+ * Registers one SAMR box (samr%levels(level)%boxes(number)); allocates its
+ * device mirror and uploads the hydro components. ghost must be 2, ncmp >= NDIM+2.
+ * Replaces the lazy per-box workspace of rhyme_mh_workspace_check
+ * (rhyme_mh_workspace_check.f90:36-77); the device holds two state buffers
+ * and no per-box workspace beyond the solver's scratch.
+ */
+int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number,
+                           double* cells, const int dims[3], int ghost,
+                           int ncmp, int* handle);
+int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle);
+
+/* Host -> device copy of the hydro components (and ghosts) of a box. */
+int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle);
+/* Device -> host copy into the registered cells array; waits for the stream
+ * (bounded wait, RHYME_GPU_ETIMEDOUT). Checks the box's status word. */
+int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle);
+
+/*
+ * dt = courant * minval(dx) / max(|v| + cs) over the box interior.
+ * Replaces pure function rhyme_cfl_time_step(c, samr)
+ * (rhyme_cfl.f90:19-23, rhyme_cfl_time_step.f90:63-84). Waits for the result.
+ */
+int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
+                            double* dt);
+
+/*
+ * Ghost fill of the 2-cell face slabs (corners untouched) with the context's
+ * boundary types. Replaces pure subroutine rhyme_samr_bc_set_boundaries
+ * (rhyme_samr_bc.f90:38-41, rhyme_samr_bc_set_boundaries.f90:9-20).
+ */
+int rhyme_gpu_set_boundaries(rhyme_gpu_ctx* ctx, int handle);
+
+/*
+ * One unsplit MUSCL-Hancock update of the box interior with time step dt.
+ * Replaces rhyme_muscl_hancock_solve (rhyme_muscl_hancock.f90:47-56,
+ * rhyme_muscl_hancock_solve.f90:3-30) and, by solver_type, its
+ * memory-intensive (rhyme_muscl_hancock_solve_memory_intensive.f90:3-181)
+ * and cpu-intensive (rhyme_muscl_hancock_solve_cpu_intensive.f90:3-159)
+ * forms. Asynchronous on the context stream.
+ */
+int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
+                       double dt);
+
+/*
+ * nsteps iterations of the driver's loop body (src/main.f90:109-136):
+ * dt from the state, ghost fill, solve, with dt kept on the device. The
+ * step is captured once in a CUDA graph and replayed. dt_trace (optional,
+ * host, nsteps entries) receives each dt. Leaves the state on the device.
+ */
+int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
+                  int nsteps, double* dt_trace);
+
+/* Waits (bounded) for all work on the context stream. */
+int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);
+
+/* ---- element-level entry points (host arrays in and out) ----------------
+ * These run the same device functions as the box solver over n independent
+ * inputs, for the Fortran interfaces Rhyme's unit tests call directly.
+ * State rows are (rho, rho*u.., e_tot), NDIM+2 doubles each.
+ */
+
+/* rhyme_riemann_problem_solve(rp, l, r, dx, dt, axis, u) for n pairs
+ * (rhyme_riemann_problem.f90:71-77, rhyme_riemann_problem_solve.f90:3-104). */
+int rhyme_gpu_riemann_solve(rhyme_gpu_ctx* ctx, const double* l,
+                            const double* r, long long n, double dx,
+                            double dt, int axis, double* u);
+
+/* p* = rhyme_irs_exec(irs, l_rho, l_v, l_p, l_cs, l_f, r_rho, r_v, r_p, r_cs,
+ * r_f, axis) (rhyme_irs.f90:22-30, rhyme_irs_exec.f90:3-45) for n rows
+ * states[n][8] = (l_rho, l_v, l_p, l_cs, r_rho, r_v, r_p, r_cs), v being the
+ * normal velocity; out[n][3] = (p*, l_f, r_f). */
+int rhyme_gpu_irs_exec(rhyme_gpu_ctx* ctx, const double* states, long long n,
+                       double* out);
+
+/* rhyme_slope_limiter_run(sl, ul, u, ur, delta) for n rows
+ * (rhyme_slope_limiter.f90:18-22, rhyme_slope_limiter_run.f90:3-20). */
+int rhyme_gpu_slope_limiter(rhyme_gpu_ctx* ctx, const double* ul,
+                            const double* u, const double* ur, long long n,
+                            double* delta);
+
+/* rhyme_muscl_hancock_half_step_extrapolation(u, delta, axis, dx, dt, l, r)
+ * for n rows (rhyme_muscl_hancock.f90:58-64,
+ * rhyme_muscl_hancock_half_step_extrapolation.f90:3-24). */
+int rhyme_gpu_half_step(rhyme_gpu_ctx* ctx, const double* u,
+                        const double* delta, long long n, int axis, double dx,
+                        double dt, double* l, double* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RHYME_GPU_H */

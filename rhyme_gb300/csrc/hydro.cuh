@@ -1,0 +1,462 @@
+// hydro.cuh -- device functions of the MUSCL-Hancock step: ideal-gas EOS,
+// slope limiters, half-step extrapolation and the exact Riemann solver.
+//
+// Templated on NDIM (D), on the normal axis (AX, compile-time so no state
+// vector is indexed dynamically) and on the arithmetic type T (double for the
+// plain path, float for the FP32 stages of the mixed path). Each routine keeps
+// the floating-point evaluation order of the Fortran routine it restates
+// (operators of equal precedence left to right), so that with FMA contraction
+// disabled the double instantiation performs the same IEEE operations as the
+// reference; the only intended difference is that the six p* guesses of
+// rhyme_irs_guess_p_star.f90 are evaluated lazily, in order, when the Newton
+// iteration from the previous guess fails (identical values, less work).
+//
+// State vectors are (rho, m_1..m_D, E); reference paths are relative to
+// Rhyme's src/.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+namespace rgpu {
+
+// ---- math by type --------------------------------------------------------
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+
+template <typename T> struct Limits;
+template <> struct Limits<double> {
+  __device__ static constexpr double tiny() { return DBL_MIN; }
+};
+template <> struct Limits<float> {
+  __device__ static constexpr float tiny() { return FLT_MIN; }
+};
+
+// Fortran MAX/MIN of two reals (same ternary as the CPU oracle).
+template <typename T> __device__ __forceinline__ T fmax_ref(T a, T b) { return (b > a) ? b : a; }
+template <typename T> __device__ __forceinline__ T fmin_ref(T a, T b) { return (b < a) ? b : a; }
+
+// Ideal-gas constants (rhyme_riemann_problem_init.f90:20-27,
+// rhyme_irs_init.f90:21-27) plus the literal quotients the reference
+// recomputes at each use (2/gp1, 2/gm1, 1/gm1_2g, gm1/2): the same values.
+template <typename T>
+struct Gas {
+  T g, gm1, gp1, gm1_gp1, gm1_2g, gp1_2g, g_inv, kb_amu;
+  T two_gp1, two_gm1, inv_gm1_2g, gm1_half, half_gm1, g_kb_amu;
+};
+
+// Run parameters used inside kernels.
+template <typename T>
+struct Rp {
+  T vac_rho, vac_p, vac_rho_next;  // w_vacuum(rho), w_vacuum(p), nearest(w_vac_rho, +1)
+  T tol;
+  int n_iter;
+};
+
+struct Limiter {
+  int type;
+  double w;
+};
+
+// ---- EOS: rhyme_hydro_base / rhyme_ideal_gas ------------------------------
+
+// rhyme_hydro_base_specific_kinetic_energy.f90:9
+template <int D, typename T>
+__device__ __forceinline__ T sp_kin_e(const T* u) {
+  T s = T(0);
+#pragma unroll
+  for (int a = 0; a < D; ++a) s = s + u[1 + a] * u[1 + a];
+  return (T(0.5) * s) / (u[0] * u[0]);
+}
+
+// rhyme_hydro_base_specific_internal_energy.f90:9
+template <int D, typename T>
+__device__ __forceinline__ T sp_int_e(const T* u) {
+  return u[D + 1] / u[0] - sp_kin_e<D>(u);
+}
+
+// rhyme_ideal_gas_pressure.f90:9
+template <int D, typename T>
+__device__ __forceinline__ T pressure(const Gas<T>& G, const T* u) {
+  return u[0] * sp_int_e<D>(u) * G.gm1;
+}
+
+// rhyme_ideal_gas_temperature_per_mu.f90:9-10, _speed_of_sound.f90:9
+template <int D, typename T>
+__device__ __forceinline__ T sound_speed(const Gas<T>& G, const T* u) {
+  T t_mu = sp_int_e<D>(u) * G.gm1 / G.kb_amu;
+  return m_sqrt(G.g_kb_amu * t_mu);
+}
+
+// rhyme_ideal_gas_flux.f90:12-23 along axis AX
+template <int D, int AX, typename T>
+__device__ __forceinline__ void flux(const Gas<T>& G, const T* u, T* f) {
+  if (m_abs(u[0]) < Limits<T>::tiny()) {
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) f[c] = T(0);
+    return;
+  }
+  T p = pressure<D>(G, u);
+  f[0] = u[1 + AX];
+#pragma unroll
+  for (int a = 0; a < D; ++a) f[1 + a] = u[1 + a] * f[0] / u[0];
+  f[1 + AX] = f[1 + AX] + p;
+  f[D + 1] = f[0] / u[0] * (u[D + 1] + p);
+}
+
+// rhyme_ideal_gas_primitive_vars_to_conserved.f90:9-11
+template <int D, typename T>
+__device__ __forceinline__ void prim_vars_to_cons(const Gas<T>& G, T rho, const T* v, T p, T* u) {
+  u[0] = rho;
+  T s = T(0);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    u[1 + a] = rho * v[a];
+    s = s + v[a] * v[a];
+  }
+  u[D + 1] = T(0.5) * rho * s + p / G.gm1;
+}
+
+// ---- slope limiter: rhyme_slope_limiter*.f90 -------------------------------
+
+// rhyme_slope_limiter_xi_r.f90:11
+template <typename T>
+__device__ __forceinline__ T xi_r(T w, T r) {
+  return T(2) / (T(1) - w + (T(1) + w) * r);
+}
+
+// r (rhyme_slope_limiter.f90:62-82) and delta of the four limiters
+// (van Leer :13-27, minmod :13-29, van Albada :13-27, superbee :13-31).
+template <typename T>
+__device__ __forceinline__ T limited_slope(int type, T w, T ul, T u, T ur) {
+  T d_L = u - ul;
+  T d_R = ur - u;
+  T d = T(0.5) * (T(1) + w) * d_L + T(0.5) * (T(1) + w) * d_R;
+  T denom = ur - u;
+  T r = (m_abs(denom) < Limits<T>::tiny()) ? T(0) : (u - ul) / denom;
+  if (type == 1) {  // van Leer
+    return (r > T(0)) ? fmin_ref(T(2) * r / (T(1) + r), xi_r(w, r)) * d : T(0);
+  } else if (type == 2) {  // minmod
+    if (r > T(1)) return fmin_ref(T(1), xi_r(w, r)) * d;
+    if (r > T(0)) return r * d;
+    return T(0);
+  } else if (type == 3) {  // van Albada; r**2.d0 folds to r*r
+    return (r > T(0)) ? fmin_ref(r * (T(1) + r) / (T(1) + r * r), xi_r(w, r)) * d : T(0);
+  } else {  // superbee
+    if (r > T(1)) return fmin_ref(fmin_ref(r, xi_r(w, r)), T(2)) * d;
+    if (r > T(0.5)) return d;
+    if (r > T(0)) return T(2) * r * d;
+    return T(0);
+  }
+}
+
+// rhyme_muscl_hancock_half_step_extrapolation.f90:15-21; hdtdx = (.5*dt)/dx
+template <int D, int AX, typename T>
+__device__ __forceinline__ void half_step(const Gas<T>& G, const T* u, const T* delta, T hdtdx,
+                                          T* l, T* r) {
+  T fl[D + 2], fr[D + 2];
+#pragma unroll
+  for (int c = 0; c < D + 2; ++c) {
+    l[c] = u[c] - T(0.5) * delta[c];
+    r[c] = u[c] + T(0.5) * delta[c];
+  }
+  flux<D, AX>(G, l, fl);
+  flux<D, AX>(G, r, fr);
+#pragma unroll
+  for (int c = 0; c < D + 2; ++c) {
+    T df = fl[c] - fr[c];
+    l[c] = l[c] + hdtdx * df;
+    r[c] = r[c] + hdtdx * df;
+  }
+}
+
+// Face states of one cell along AX from its neighbours um, u0, up.
+template <int D, int AX, typename T>
+__device__ __forceinline__ void face_states(const Gas<T>& G, int lim, T w, const T* um, const T* u0,
+                                            const T* up, T hdtdx, T* l, T* r) {
+  T delta[D + 2];
+#pragma unroll
+  for (int c = 0; c < D + 2; ++c) delta[c] = limited_slope(lim, w, um[c], u0[c], up[c]);
+  half_step<D, AX>(G, u0, delta, hdtdx, l, r);
+}
+
+// ---- exact Riemann solver: rhyme_irs_*, rhyme_riemann_problem_* -----------
+
+// rhyme_irs_nonlinear_wave_function.f90:13-24
+template <typename T>
+__device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, T s_rho, T s_p, T s_cs, T p, T& f,
+                                               T& fprime) {
+  if (p > s_p) {
+    T Ak = T(2) / (G.gp1 * s_rho);
+    T Bk = G.gm1 * s_p / G.gp1;
+    T factor = m_sqrt(Ak / (Bk + p));
+    f = (p - s_p) * factor;
+    fprime = factor * (T(1) - (p - s_p) / (T(2) * (Bk + p)));
+  } else {
+    f = T(2) * s_cs / G.gm1 * (m_pow(p / s_p, G.gm1_2g) - T(1));
+    fprime = T(1) / (s_rho * s_cs) * m_pow(p / s_p, -G.gp1_2g);
+  }
+}
+
+// Guess number k (0..5) of rhyme_irs_guess_p_star.f90:14-71, floored at tiny.
+template <typename T>
+__device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T l_p, T l_cs, T r_rho,
+                                       T vr, T r_p, T r_cs) {
+  T p;
+  if (k == 0) {
+    const T q_user = T(2);
+    T cup = T(0.25) * (l_rho + r_rho) * (l_cs + r_cs);
+    T ppv = fmax_ref(T(0.5) * (l_p + r_p) + T(0.5) * (vl - vr) * cup, T(0));
+    T p_min = fmin_ref(l_p, r_p);
+    T p_max = fmax_ref(l_p, r_p);
+    T q_max = p_max / p_min;
+    if (q_max <= q_user && (p_min < ppv && ppv < p_max)) {
+      p = ppv;  // PVRS
+    } else if (ppv < p_min) {  // two-rarefaction
+      T pq = m_pow(l_p / r_p, G.gm1_2g);
+      T um = (pq * vl / l_cs + vr / r_cs + G.two_gm1 * (pq - T(1))) / (pq / l_cs + T(1) / r_cs);
+      T ptl = T(1) + G.half_gm1 * (vl - um) / l_cs;
+      T ptr = T(1) + G.half_gm1 * (um - vr) / r_cs;
+      p = T(0.5) * (l_p * m_pow(ptl, G.inv_gm1_2g) + r_p * m_pow(ptr, G.inv_gm1_2g));
+    } else {  // two-shock
+      T gel = m_sqrt((G.two_gp1 / l_rho) / (G.gm1_gp1 * l_p + ppv));
+      T ger = m_sqrt((G.two_gp1 / r_rho) / (G.gm1_gp1 * r_p + ppv));
+      p = (gel * l_p + ger * r_p - (vr - vl)) / (gel + ger);
+    }
+  } else if (k == 1) {  // Ramses
+    p = (r_rho * r_cs * l_p + l_rho * l_cs * r_p + r_cs * l_cs * (l_rho * vl - r_rho * vr)) /
+        (r_rho * r_cs + l_rho * l_cs);
+  } else if (k == 2) {  // two-rarefaction approximation
+    p = m_pow((l_cs + r_cs - G.gm1_half * (vr - vl)) /
+                  (m_pow(l_cs / l_p, G.gm1_2g) + m_pow(r_cs / r_p, G.gm1_2g)),
+              G.inv_gm1_2g);
+  } else if (k == 3) {  // two-shock approximation; g_K at :74-80
+    T l_g = m_sqrt((T(2) / (G.gp1 * l_rho)) / (l_p + G.gm1_gp1 * l_p));
+    T r_g = m_sqrt((T(2) / (G.gp1 * r_rho)) / (r_p + G.gm1_gp1 * r_p));
+    p = (l_g * l_p + r_g * r_p - (vr - vl)) / (l_g + r_g);
+  } else if (k == 4) {  // p_PV
+    p = T(0.5) * (l_p + r_p) - T(0.125) * (vr - vl) * (l_rho + r_rho) * (l_cs + r_cs);
+  } else {  // arithmetic mean
+    p = T(0.5) * (l_p + r_p);
+  }
+  return fmax_ref(p, Limits<T>::tiny());
+}
+
+// rhyme_irs_exec.f90:19-44 with lazily evaluated guesses. l_f / r_f are the
+// wave functions at the last iterate before the final update.
+template <typename T>
+__device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
+                                      T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f) {
+  T p_star = T(0), p_prev, l_fp, r_fp;
+  for (int gid = 0; gid < 6; ++gid) {
+    p_star = guess_p_star(G, gid, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
+    p_prev = p_star;
+    for (int i = 1; i <= n_iter; ++i) {
+      nonlinear_wave(G, l_rho, l_p, l_cs, p_star, l_f, l_fp);
+      nonlinear_wave(G, r_rho, r_p, r_cs, p_star, r_f, r_fp);
+      p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
+      if (p_star < T(0)) break;
+      if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) break;
+      p_prev = p_star;
+    }
+    if (p_star > T(0)) break;
+  }
+  if (p_star < T(0)) p_star = T(0);
+  return p_star;
+}
+
+// rp_side_t (rhyme_riemann_problem.f90:53-56)
+template <int D, typename T>
+struct Side {
+  T rho, v[D], p, cs;
+};
+
+// Sampled star-region summary (rhyme_riemann_problem.f90:33-51).
+template <typename T>
+struct Star {
+  T u, p;
+  bool l_shock, r_shock;
+  T l_rho, l_speed, l_cs, l_speedH, l_speedT;  // speed = shock speed
+  T r_rho, r_speed, r_cs, r_speedH, r_speedT;
+  T l_f, r_f;
+};
+
+// rhyme_riemann_problem_star.f90:12-65
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
+                                        const Side<D, T>& R, Star<T>& s) {
+  s.p = irs_exec(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
+                 s.r_f);
+  if (s.p < rp.vac_p) s.p = rp.vac_p;
+  s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
+  T ps_pl = s.p / L.p;
+  T ps_pr = s.p / R.p;
+  if (s.p > L.p) {
+    s.l_shock = true;
+    s.l_rho = L.rho * (G.gm1_gp1 + ps_pl) / (G.gm1_gp1 * ps_pl + T(1));
+    s.l_speed = L.v[AX] - L.cs * m_sqrt(G.gp1_2g * ps_pl + G.gm1_2g);
+  } else {
+    s.l_shock = false;
+    s.l_rho = L.rho * m_pow(ps_pl, G.g_inv);
+    s.l_cs = L.cs * m_pow(ps_pl, G.gm1_2g);
+    s.l_speedH = L.v[AX] - L.cs;
+    s.l_speedT = s.u - s.l_cs;
+  }
+  if (s.p > R.p) {
+    s.r_shock = true;
+    s.r_rho = R.rho * (G.gm1_gp1 + ps_pr) / (G.gm1_gp1 * ps_pr + T(1));
+    s.r_speed = R.v[AX] + R.cs * m_sqrt(G.gp1_2g * ps_pr + G.gm1_2g);
+  } else {
+    s.r_shock = false;
+    s.r_rho = R.rho * m_pow(ps_pr, G.g_inv);
+    s.r_cs = R.cs * m_pow(ps_pr, G.gm1_2g);
+    s.r_speedH = R.v[AX] + R.cs;
+    s.r_speedT = s.u + s.r_cs;
+  }
+}
+
+// rhyme_riemann_problem_w_kfan.f90:14-31
+template <int D, int AX, typename T>
+__device__ __noinline__ void w_kfan(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
+  T cs = is_right ? -s.cs : s.cs;
+  T rho = s.rho * m_pow(G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt), G.two_gm1);
+  T v[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = s.v[a];
+  v[AX] = G.two_gp1 * (cs + G.half_gm1 * s.v[AX] + dxdt);
+  T p = s.p * m_pow(G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt), G.inv_gm1_2g);
+  prim_vars_to_cons<D>(G, rho, v, p, u);
+}
+
+// rhyme_riemann_problem_w_star{L,R}_{sho,fan}.f90:12-15
+template <int D, int AX, typename T>
+__device__ __forceinline__ void w_star(const Gas<T>& G, const Side<D, T>& side, const Star<T>& s, T rho,
+                                       T* u) {
+  T v[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = side.v[a];
+  v[AX] = s.u;
+  prim_vars_to_cons<D>(G, rho, v, s.p, u);
+}
+
+// rhyme_riemann_problem_sampling.f90:13-47 at x/t = dxdt
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_sampling(const Gas<T>& G, const Side<D, T>& L, const Side<D, T>& R,
+                                            const Star<T>& s, T dxdt, T* u) {
+  if (dxdt > s.u) {
+    if (s.r_shock) {
+      if (dxdt < s.r_speed) w_star<D, AX>(G, R, s, s.r_rho, u);
+      else prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
+    } else {
+      if (dxdt < s.r_speedT) w_star<D, AX>(G, R, s, s.r_rho, u);
+      else if (dxdt < s.r_speedH) w_kfan<D, AX>(G, R, dxdt, true, u);
+      else prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
+    }
+  } else {
+    if (s.l_shock) {
+      if (dxdt > s.l_speed) w_star<D, AX>(G, L, s, s.l_rho, u);
+      else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
+    } else {
+      if (dxdt > s.l_speedT) w_star<D, AX>(G, L, s, s.l_rho, u);
+      else if (dxdt > s.l_speedH) w_kfan<D, AX>(G, L, dxdt, false, u);
+      else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
+    }
+  }
+}
+
+// Vacuum state W_0: prim_to_cons of w_vacuum (rho, 0.., p).
+template <int D, typename T>
+__device__ __forceinline__ void vacuum_state(const Gas<T>& G, const Rp<T>& rp, T* u) {
+  T v[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = T(0);
+  prim_vars_to_cons<D>(G, rp.vac_rho, v, rp.vac_p, u);
+}
+
+// rhyme_riemann_problem_solve.f90:17-103 sampled at x/t = dxdt.
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
+                                         T dxdt, T* u) {
+  Side<D, T> L, R;
+  L.rho = fmax_ref(l[0], rp.vac_rho);
+  R.rho = fmax_ref(r[0], rp.vac_rho);
+  const T e_rho = rp.vac_rho_next;
+  const bool vacuum_right = R.rho < e_rho && L.rho > e_rho;
+  const bool vacuum_left = L.rho < e_rho && R.rho > e_rho;
+  const bool vacuum_both = L.rho < e_rho && R.rho < e_rho;
+  const T tiny = Limits<T>::tiny();
+
+  if (vacuum_right) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) L.v[a] = l[1 + a] / l[0];
+    L.p = fmax_ref(pressure<D>(G, l), rp.vac_p);
+    L.cs = fmax_ref(sound_speed<D>(G, l), tiny);
+#pragma unroll
+    for (int a = 0; a < D; ++a) R.v[a] = T(0);
+    R.p = rp.vac_p;
+    R.cs = T(0);
+    T s_starl = L.v[AX] - T(2) * L.cs / G.gm1;
+    if (dxdt > s_starl) vacuum_state<D>(G, rp, u);
+    else if (dxdt > L.v[AX] - L.cs) w_kfan<D, AX>(G, L, dxdt, false, u);
+    else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
+  } else if (vacuum_left) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) L.v[a] = T(0);
+    L.p = rp.vac_p;
+    L.cs = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) R.v[a] = r[1 + a] / r[0];
+    R.p = fmax_ref(pressure<D>(G, r), rp.vac_p);
+    R.cs = fmax_ref(sound_speed<D>(G, r), tiny);
+    T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
+    if (dxdt > R.v[AX] + R.cs) prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
+    else if (dxdt > s_starr) w_kfan<D, AX>(G, R, dxdt, true, u);
+    else vacuum_state<D>(G, rp, u);
+  } else if (vacuum_both) {
+    vacuum_state<D>(G, rp, u);
+  } else {
+#pragma unroll
+    for (int a = 0; a < D; ++a) L.v[a] = l[1 + a] / l[0];
+    L.p = fmax_ref(pressure<D>(G, l), rp.vac_p);
+    L.cs = fmax_ref(sound_speed<D>(G, l), tiny);
+#pragma unroll
+    for (int a = 0; a < D; ++a) R.v[a] = r[1 + a] / r[0];
+    R.p = fmax_ref(pressure<D>(G, r), rp.vac_p);
+    R.cs = fmax_ref(sound_speed<D>(G, r), tiny);
+    T s_starl = L.v[AX] - T(2) * L.cs / G.gm1;
+    T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
+    T du = R.v[AX] - L.v[AX];
+    T du_crit = T(2) * (L.cs + R.cs) / G.gm1;
+    if (du_crit < du) {  // vacuum generation
+      if (dxdt > s_starr) {
+        if (dxdt > R.v[AX] + R.cs) prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
+        else w_kfan<D, AX>(G, R, dxdt, true, u);
+      } else if (dxdt > s_starl) {
+        vacuum_state<D>(G, rp, u);
+      } else {
+        if (dxdt > L.v[AX] - L.cs) w_kfan<D, AX>(G, L, dxdt, false, u);
+        else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
+      }
+    } else {
+      Star<T> s;
+      rp_star<D, AX>(G, rp, L, R, s);
+      rp_sampling<D, AX>(G, L, R, s, dxdt, u);
+    }
+  }
+}
+
+// Interface flux: Riemann state at x/t = 0 (dx = 0 in
+// rhyme_muscl_hancock_solve_memory_intensive.f90:110-116), then calc_flux.
+template <int D, int AX, typename T>
+__device__ __forceinline__ void interface_flux(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
+                                               T* f) {
+  T u[D + 2];
+  rp_solve<D, AX>(G, rp, l, r, T(0), u);
+  flux<D, AX>(G, u, f);
+}
+
+}  // namespace rgpu

@@ -1,0 +1,89 @@
+// rgpu_internal.h -- types shared by the kernels and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hydro.cuh"
+
+namespace rgpu {
+
+// Per-run parameters passed by value to every kernel.
+struct DevParams {
+  Gas<double> G;
+  Rp<double> rp;
+  int ndim;
+  int limiter;
+  double omega;
+  int solver_type;
+  int bc[6];
+  double inflow[6][5];
+  double courant;
+};
+
+// Geometry of one box in the reference layout: component blocks of
+// `field` doubles, cell (i,j,k) (1-based interior, ghosts -1..N+2) at
+// (i+1)*s0 + (j+1)*s1 + (k+1)*s2 for the active axes.
+struct Geom {
+  int n[3];          // interior cells per axis (1 beyond NDIM)
+  long long s[3];    // element strides per axis
+  long long field;   // elements per component block
+  __host__ __device__ long long at(int D, int i, int j, int k) const {
+    long long o = (long long)(i + 1) * s[0];
+    if (D > 1) o += (long long)(j + 1) * s[1];
+    if (D > 2) o += (long long)(k + 1) * s[2];
+    return o;
+  }
+};
+
+inline Geom make_geom(int D, const int* dims) {
+  Geom g;
+  int ext[3];
+  for (int a = 0; a < 3; ++a) {
+    g.n[a] = (a < D) ? dims[a] : 1;
+    ext[a] = (a < D) ? dims[a] + 4 : 1;
+  }
+  g.s[0] = 1;
+  g.s[1] = ext[0];
+  g.s[2] = (long long)ext[0] * ext[1];
+  g.field = g.s[2] * ext[2];
+  return g;
+}
+
+// Device scratch of one box for the plain FP64 solver.
+struct StepScratch {
+  double* faces = nullptr;   // [D][2][D+2][field]: ul, ur per axis
+  double* fluxes = nullptr;  // [D][D+2][field]
+  double* dt = nullptr;      // current dt (device scalar)
+  unsigned long long* max_bits = nullptr;  // CFL max, as bits (self-resetting)
+  unsigned int* counter = nullptr;         // CFL finished-block counter (self-resetting)
+  int* status = nullptr;                   // sticky status bits (1: NaN/Inf or rho <= 0)
+  double* dt_trace = nullptr;              // optional device dt trace
+  int* trace_pos = nullptr;                // next trace slot
+  int trace_cap = 0;
+};
+
+struct Dx {
+  double v[3];
+  double min;  // minval(dx(1:NDIM))
+};
+
+// Launchers (kernels_box.cu). All asynchronous on `st`.
+cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,
+                              cudaStream_t st);
+cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const Dx& dx,
+                       const StepScratch& s, cudaStream_t st);
+cudaError_t launch_mh_solve(const DevParams& P, const double* U, double* Unew, const Geom& g,
+                            const Dx& dx, const StepScratch& s, cudaStream_t st);
+int max_cfl_blocks();
+
+// Element-level launchers (kernels_elem.cu): device arrays in and out.
+cudaError_t launch_riemann_solve(const DevParams& P, const double* l, const double* r, long long n,
+                                 double dxdt, int axis, double* u, cudaStream_t st);
+cudaError_t launch_irs_exec(const DevParams& P, const double* states, long long n, double* out,
+                            cudaStream_t st);
+cudaError_t launch_slope_limiter(const DevParams& P, const double* ul, const double* u,
+                                 const double* ur, long long n, double* delta, cudaStream_t st);
+cudaError_t launch_half_step(const DevParams& P, const double* u, const double* delta, long long n,
+                             int axis, double hdtdx, double* l, double* r, cudaStream_t st);
+
+}  // namespace rgpu

@@ -1,0 +1,568 @@
+// rhyme_gpu.cu -- host side of the C-ABI (include/rhyme_gpu.h).
+//
+// A context holds the run parameters (the values of Rhyme's solver modules),
+// one CUDA stream and a registry of boxes. Each box owns two device state
+// buffers (ping-pong: the unsplit update reads U^n and writes U^{n+1}), the
+// solver scratch, and up to two captured CUDA graphs of one driver step (one
+// per buffer parity) that rhyme_gpu_run replays.
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/rhyme_gpu.h"
+#include "rgpu_internal.h"
+
+using namespace rgpu;
+
+namespace {
+
+struct Box {
+  int level = 0, number = 0;
+  double* host = nullptr;
+  int dims[3] = {1, 1, 1};
+  int ncmp = 0;
+  Geom g{};
+  size_t hydro_bytes = 0;  // (NDIM+2) component blocks
+  double* state[2] = {nullptr, nullptr};
+  int cur = 0;
+  StepScratch s{};
+  double* trace_buf = nullptr;
+  int* trace_pos = nullptr;
+  bool registered_host = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  Dx graph_dx{};
+  bool graph_valid = false;
+};
+
+}  // namespace
+
+struct rhyme_gpu_ctx {
+  rhyme_gpu_params params{};
+  DevParams dp{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<Box*> boxes;
+  double* pinned_dt = nullptr;   // pinned host scalar for dt up/down loads
+  void* elem_buf = nullptr;      // growable device buffer for element calls
+  size_t elem_cap = 0;
+  double timeout_s = 600.0;
+};
+
+namespace {
+
+constexpr int kTraceCap = 4096;
+
+int fail(rhyme_gpu_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? RHYME_GPU_ENOMEM : RHYME_GPU_ECUDA, \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+  } while (0)
+
+// Bounded wait on the context stream: polls an event until the deadline.
+int wait_stream(rhyme_gpu_ctx* ctx) {
+  cudaEvent_t ev;
+  CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, ctx->stream);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(ev);
+    return fail(ctx, RHYME_GPU_ECUDA, "cudaEventRecord: %s", cudaGetErrorString(e));
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  int spins = 0;
+  for (;;) {
+    e = cudaEventQuery(ev);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) {
+      cudaEventDestroy(ev);
+      return fail(ctx, RHYME_GPU_ECUDA, "stream wait: %s", cudaGetErrorString(e));
+    }
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > ctx->timeout_s) {
+      cudaEventDestroy(ev);
+      return fail(ctx, RHYME_GPU_ETIMEDOUT, "stream wait exceeded %.0f s", ctx->timeout_s);
+    }
+    if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  cudaEventDestroy(ev);
+  return RHYME_GPU_OK;
+}
+
+Box* find_box(rhyme_gpu_ctx* ctx, int handle) {
+  if (handle < 0 || handle >= (int)ctx->boxes.size()) return nullptr;
+  return ctx->boxes[handle];
+}
+
+int validate(rhyme_gpu_ctx* ctx, const rhyme_gpu_params* p) {
+  if (p->ndim < 1 || p->ndim > 3) return fail(ctx, RHYME_GPU_EINVAL, "ndim must be 1, 2 or 3 (got %d)", p->ndim);
+  if (p->limiter < 1 || p->limiter > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown slope limiter %d", p->limiter);
+  if (p->solver_type != RHYME_GPU_CPU_INTENSIVE && p->solver_type != RHYME_GPU_MEMORY_INTENSIVE)
+    return fail(ctx, RHYME_GPU_EINVAL, "Unknown solver type %d", p->solver_type);
+  if (p->precision != RHYME_GPU_FP64 && p->precision != RHYME_GPU_MIXED)
+    return fail(ctx, RHYME_GPU_EINVAL, "unknown precision mode %d", p->precision);
+  if (p->n_iteration < 0) return fail(ctx, RHYME_GPU_EINVAL, "n_iteration must be >= 0");
+  if (!(p->gamma > 1.0)) return fail(ctx, RHYME_GPU_EINVAL, "gamma must exceed 1");
+  if (!(p->kb_amu > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "kb_amu must be positive");
+  if (!(p->courant > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "courant number must be positive");
+  for (int i = 0; i < 2 * p->ndim; ++i)
+    if (p->bc[i] < 1 || p->bc[i] > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d on side %d", p->bc[i], i + 1);
+  return RHYME_GPU_OK;
+}
+
+void make_dev_params(const rhyme_gpu_params* p, DevParams* d) {
+  memset(d, 0, sizeof(*d));
+  const double g = p->gamma;
+  Gas<double>& G = d->G;
+  G.g = g;
+  G.gm1 = g - 1.0;
+  G.gp1 = g + 1.0;
+  G.gm1_gp1 = G.gm1 / G.gp1;
+  G.gm1_2g = G.gm1 / (2.0 * g);
+  G.gp1_2g = G.gp1 / (2.0 * g);
+  G.g_inv = 1.0 / g;
+  G.kb_amu = p->kb_amu;
+  G.two_gp1 = 2.0 / G.gp1;
+  G.two_gm1 = 2.0 / G.gm1;
+  G.inv_gm1_2g = 1.0 / G.gm1_2g;
+  G.gm1_half = 0.5 * G.gm1;
+  G.half_gm1 = G.gm1 / 2.0;
+  G.g_kb_amu = g * p->kb_amu;
+  d->rp.vac_rho = p->vacuum_density;
+  d->rp.vac_p = p->vacuum_pressure;
+  d->rp.vac_rho_next = std::nextafter(p->vacuum_density, 1.0);
+  d->rp.tol = p->tolerance;
+  d->rp.n_iter = p->n_iteration;
+  d->ndim = p->ndim;
+  d->limiter = p->limiter;
+  d->omega = p->omega;
+  d->solver_type = p->solver_type;
+  for (int i = 0; i < 6; ++i) {
+    d->bc[i] = (i < 2 * p->ndim) ? p->bc[i] : 0;
+    for (int c = 0; c < 5; ++c) d->inflow[i][c] = p->inflow[i][c];
+  }
+  d->courant = p->courant;
+}
+
+void destroy_box(Box* b) {
+  if (!b) return;
+  for (int i = 0; i < 2; ++i) {
+    if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+    cudaFree(b->state[i]);
+  }
+  cudaFree(b->s.faces);
+  cudaFree(b->s.fluxes);
+  cudaFree(b->s.dt);
+  if (b->registered_host) cudaHostUnregister(b->host);
+  delete b;
+}
+
+Dx make_dx(int D, const double dx[3]) {
+  Dx d;
+  for (int a = 0; a < 3; ++a) d.v[a] = (a < D) ? dx[a] : 1.0;
+  // minval(samr%levels(0)%dx), rhyme_cfl_time_step.f90:74
+  d.min = d.v[0];
+  for (int a = 1; a < D; ++a)
+    if (d.v[a] < d.min) d.min = d.v[a];
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rhyme_gpu_abi_version(void) { return RHYME_GPU_ABI_VERSION; }
+
+int rhyme_gpu_create(rhyme_gpu_ctx** out, const rhyme_gpu_params* params) {
+  if (!out || !params) return RHYME_GPU_EINVAL;
+  *out = nullptr;
+  rhyme_gpu_ctx* ctx = new rhyme_gpu_ctx();
+  int rc = validate(ctx, params);
+  if (rc != RHYME_GPU_OK) {
+    fprintf(stderr, "rhyme_gpu_create: %s\n", ctx->err.c_str());
+    delete ctx;
+    return rc;
+  }
+  ctx->params = *params;
+  make_dev_params(params, &ctx->dp);
+  const char* to = getenv("RHYME_GPU_TIMEOUT_S");
+  if (to && atof(to) > 0) ctx->timeout_s = atof(to);
+  cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->pinned_dt, sizeof(double) * 8);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "rhyme_gpu_create: %s\n", cudaGetErrorString(e));
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RHYME_GPU_ECUDA;
+  }
+  *out = ctx;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_destroy(rhyme_gpu_ctx* ctx) {
+  if (!ctx) return RHYME_GPU_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (Box* b : ctx->boxes) destroy_box(b);
+  cudaFree(ctx->elem_buf);
+  cudaFreeHost(ctx->pinned_dt);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return RHYME_GPU_OK;
+}
+
+const char* rhyme_gpu_last_error(const rhyme_gpu_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int rhyme_gpu_get_stream(rhyme_gpu_ctx* ctx, void** stream) {
+  if (!ctx || !stream) return RHYME_GPU_EINVAL;
+  *stream = (void*)ctx->stream;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  return wait_stream(ctx);
+}
+
+int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* cells,
+                           const int dims[3], int ghost, int ncmp, int* handle) {
+  if (!ctx || !cells || !dims || !handle) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  const int D = ctx->params.ndim;
+  if (ghost != 2) return fail(ctx, RHYME_GPU_EINVAL, "ghost width must be 2 (got %d)", ghost);
+  if (ncmp < D + 2) return fail(ctx, RHYME_GPU_EINVAL, "ncmp %d < NDIM+2", ncmp);
+  for (int a = 0; a < 3; ++a) {
+    if (a < D && dims[a] < 1) return fail(ctx, RHYME_GPU_EINVAL, "dims(%d) must be >= 1", a + 1);
+    if (a >= D && dims[a] != 1) return fail(ctx, RHYME_GPU_EINVAL, "dims(%d) must be 1 beyond NDIM", a + 1);
+  }
+  Box* b = new Box();
+  b->level = level;
+  b->number = number;
+  b->host = cells;
+  b->ncmp = ncmp;
+  for (int a = 0; a < 3; ++a) b->dims[a] = dims[a];
+  b->g = make_geom(D, dims);
+  const long long F = b->g.field;
+  b->hydro_bytes = (size_t)(D + 2) * F * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->state[i], b->hydro_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double));
+  // small block: dt, max_bits, counter, status, trace_pos, then the trace
+  const size_t small = 64 + sizeof(double) * kTraceCap;
+  if (e == cudaSuccess) e = cudaMalloc(&b->s.dt, small);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->s.dt, 0, small, ctx->stream);
+  if (e != cudaSuccess) {
+    destroy_box(b);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? RHYME_GPU_ENOMEM : RHYME_GPU_ECUDA,
+                "box allocation: %s", cudaGetErrorString(e));
+  }
+  char* base = (char*)b->s.dt;
+  b->s.max_bits = (unsigned long long*)(base + 8);
+  b->s.counter = (unsigned int*)(base + 16);
+  b->s.status = (int*)(base + 20);
+  b->trace_pos = (int*)(base + 24);
+  b->trace_buf = (double*)(base + 64);
+  // Pin the caller's array for asynchronous copies when possible; a failure
+  // here only costs copy speed.
+  if (cudaHostRegister(cells, (size_t)ncmp * F * sizeof(double), cudaHostRegisterDefault) == cudaSuccess)
+    b->registered_host = true;
+  else
+    cudaGetLastError();
+  ctx->boxes.push_back(b);
+  *handle = (int)ctx->boxes.size() - 1;
+  return rhyme_gpu_sync_to_device(ctx, *handle);
+}
+
+int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  cudaStreamSynchronize(ctx->stream);
+  destroy_box(b);
+  ctx->boxes[handle] = nullptr;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  // Both buffers receive the full hydro blocks (ghosts and corners included).
+  CK(cudaMemcpyAsync(b->state[b->cur], b->host, b->hydro_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(b->state[1 - b->cur], b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToDevice,
+                     ctx->stream));
+  if (!b->registered_host) return wait_stream(ctx);
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  int* st = (int*)(ctx->pinned_dt + 1);
+  CK(cudaMemcpyAsync(st, b->s.status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemsetAsync(b->s.status, 0, sizeof(int), ctx->stream));
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  if (*st & 1)
+    return fail(ctx, RHYME_GPU_ENANSTATE,
+                "box (level %d, number %d) holds NaN/Inf or non-positive density", b->level, b->number);
+  return RHYME_GPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Step entry points
+// ---------------------------------------------------------------------------
+namespace {
+
+StepScratch scratch_of(Box* b, bool trace) {
+  StepScratch s = b->s;
+  s.dt_trace = trace ? b->trace_buf : nullptr;
+  s.trace_pos = b->trace_pos;
+  s.trace_cap = trace ? kTraceCap : 0;
+  return s;
+}
+
+// One driver step on the device: dt (into s.dt), ghost fill of U (mirrored
+// into the other buffer), solve U -> other buffer.
+cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool trace) {
+  StepScratch s = scratch_of(b, trace);
+  double* U = b->state[cur];
+  double* V = b->state[1 - cur];
+  cudaError_t e = launch_cfl(ctx->dp, U, b->g, dx, s, ctx->stream);
+  if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
+  if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, dx, s, ctx->stream);
+  return e;
+}
+
+int ensure_graphs(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
+  if (b->graph_valid && memcmp(&b->graph_dx, &dx, sizeof(Dx)) == 0) return RHYME_GPU_OK;
+  for (int i = 0; i < 2; ++i) {
+    if (b->graph[i]) {
+      cudaGraphExecDestroy(b->graph[i]);
+      b->graph[i] = nullptr;
+    }
+  }
+  for (int parity = 0; parity < 2; ++parity) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_step(ctx, b, parity, dx, true);
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (e2 == cudaSuccess) cudaGraphDestroy(graph);
+      return fail(ctx, RHYME_GPU_ECUDA, "graph capture: %s",
+                  cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&b->graph[parity], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e3 != cudaSuccess) return fail(ctx, RHYME_GPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e3));
+  }
+  b->graph_dx = dx;
+  b->graph_valid = true;
+  return RHYME_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], double* dt) {
+  if (!ctx || !dx || !dt) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  Dx d = make_dx(ctx->params.ndim, dx);
+  CK(launch_cfl(ctx->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
+  CK(cudaMemcpyAsync(ctx->pinned_dt, b->s.dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  *dt = ctx->pinned_dt[0];
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_set_boundaries(rhyme_gpu_ctx* ctx, int handle) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  CK(launch_ghost_fill(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, ctx->stream));
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], double dt) {
+  if (!ctx || !dx) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(ctx, RHYME_GPU_EINVAL, "dt must be positive and finite");
+  Dx d = make_dx(ctx->params.ndim, dx);
+  // The pinned staging scalar may still be read by an earlier copy; wait for
+  // it before reuse (cheap: the stream is usually idle at this point).
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  ctx->pinned_dt[0] = dt;
+  CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_mh_solve(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
+                     ctx->stream));
+  b->cur = 1 - b->cur;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int nsteps, double* dt_trace) {
+  if (!ctx || !dx) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  if (nsteps < 0) return fail(ctx, RHYME_GPU_EINVAL, "nsteps must be >= 0");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  Dx d = make_dx(ctx->params.ndim, dx);
+  int rc = ensure_graphs(ctx, b, d);
+  if (rc != RHYME_GPU_OK) return rc;
+  int done = 0;
+  while (done < nsteps) {
+    const int chunk = (nsteps - done < kTraceCap) ? nsteps - done : kTraceCap;
+    CK(cudaMemsetAsync(b->trace_pos, 0, sizeof(int), ctx->stream));
+    for (int s = 0; s < chunk; ++s) {
+      CK(cudaGraphLaunch(b->graph[b->cur], ctx->stream));
+      b->cur = 1 - b->cur;
+    }
+    if (dt_trace) {
+      CK(cudaMemcpyAsync(dt_trace + done, b->trace_buf, sizeof(double) * chunk, cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      rc = wait_stream(ctx);
+      if (rc != RHYME_GPU_OK) return rc;
+    }
+    done += chunk;
+  }
+  return RHYME_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Element-level entry points
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+int elem_reserve(rhyme_gpu_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->elem_cap) return RHYME_GPU_OK;
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  cudaFree(ctx->elem_buf);
+  ctx->elem_buf = nullptr;
+  ctx->elem_cap = 0;
+  CK(cudaMalloc(&ctx->elem_buf, bytes));
+  ctx->elem_cap = bytes;
+  return RHYME_GPU_OK;
+}
+
+// Copies `nin` host arrays of in_sz[i] bytes to the device, runs `launch`
+// with the device pointers, copies `nout` results back and waits.
+template <typename F>
+int elem_call(rhyme_gpu_ctx* ctx, int nin, const void* const* in, const size_t* in_sz, int nout,
+              void* const* out, const size_t* out_sz, F launch) {
+  size_t total = 0;
+  size_t off[8];
+  for (int i = 0; i < nin + nout; ++i) {
+    off[i] = total;
+    total += ((i < nin ? in_sz[i] : out_sz[i - nin]) + 255) & ~(size_t)255;
+  }
+  int rc = elem_reserve(ctx, total > 0 ? total : 256);
+  if (rc != RHYME_GPU_OK) return rc;
+  char* base = (char*)ctx->elem_buf;
+  for (int i = 0; i < nin; ++i)
+    CK(cudaMemcpyAsync(base + off[i], in[i], in_sz[i], cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch(base, off));
+  for (int i = 0; i < nout; ++i)
+    CK(cudaMemcpyAsync(out[i], base + off[nin + i], out_sz[i], cudaMemcpyDeviceToHost, ctx->stream));
+  return wait_stream(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rhyme_gpu_riemann_solve(rhyme_gpu_ctx* ctx, const double* l, const double* r, long long n,
+                            double dx, double dt, int axis, double* u) {
+  if (!ctx || n < 0 || (n > 0 && (!l || !r || !u))) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  if (axis < 0 || axis >= ctx->params.ndim) return fail(ctx, RHYME_GPU_EINVAL, "axis %d out of range", axis);
+  if (n == 0) return RHYME_GPU_OK;
+  const size_t sz = (size_t)n * (ctx->params.ndim + 2) * sizeof(double);
+  const void* in[2] = {l, r};
+  size_t isz[2] = {sz, sz};
+  void* out[1] = {u};
+  size_t osz[1] = {sz};
+  const double dxdt = dx / dt;  // rhyme_riemann_problem_solve.f90:17
+  DevParams P = ctx->dp;
+  return elem_call(ctx, 2, in, isz, 1, out, osz, [&](char* base, const size_t* off) {
+    return launch_riemann_solve(P, (const double*)(base + off[0]), (const double*)(base + off[1]), n, dxdt,
+                                axis, (double*)(base + off[2]), ctx->stream);
+  });
+}
+
+int rhyme_gpu_irs_exec(rhyme_gpu_ctx* ctx, const double* states, long long n, double* out3) {
+  if (!ctx || n < 0 || (n > 0 && (!states || !out3))) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  if (n == 0) return RHYME_GPU_OK;
+  const void* in[1] = {states};
+  size_t isz[1] = {(size_t)n * 8 * sizeof(double)};
+  void* out[1] = {out3};
+  size_t osz[1] = {(size_t)n * 3 * sizeof(double)};
+  DevParams P = ctx->dp;
+  return elem_call(ctx, 1, in, isz, 1, out, osz, [&](char* base, const size_t* off) {
+    return launch_irs_exec(P, (const double*)(base + off[0]), n, (double*)(base + off[1]), ctx->stream);
+  });
+}
+
+int rhyme_gpu_slope_limiter(rhyme_gpu_ctx* ctx, const double* ul, const double* u, const double* ur,
+                            long long n, double* delta) {
+  if (!ctx || n < 0 || (n > 0 && (!ul || !u || !ur || !delta))) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  if (n == 0) return RHYME_GPU_OK;
+  const long long m = n * (ctx->params.ndim + 2);
+  const size_t sz = (size_t)m * sizeof(double);
+  const void* in[3] = {ul, u, ur};
+  size_t isz[3] = {sz, sz, sz};
+  void* out[1] = {delta};
+  size_t osz[1] = {sz};
+  DevParams P = ctx->dp;
+  return elem_call(ctx, 3, in, isz, 1, out, osz, [&](char* base, const size_t* off) {
+    return launch_slope_limiter(P, (const double*)(base + off[0]), (const double*)(base + off[1]),
+                                (const double*)(base + off[2]), m, (double*)(base + off[3]), ctx->stream);
+  });
+}
+
+int rhyme_gpu_half_step(rhyme_gpu_ctx* ctx, const double* u, const double* delta, long long n, int axis,
+                        double dx, double dt, double* l, double* r) {
+  if (!ctx || n < 0 || (n > 0 && (!u || !delta || !l || !r))) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  if (axis < 0 || axis >= ctx->params.ndim) return fail(ctx, RHYME_GPU_EINVAL, "axis %d out of range", axis);
+  if (n == 0) return RHYME_GPU_OK;
+  const size_t sz = (size_t)n * (ctx->params.ndim + 2) * sizeof(double);
+  const void* in[2] = {u, delta};
+  size_t isz[2] = {sz, sz};
+  void* out[2] = {l, r};
+  size_t osz[2] = {sz, sz};
+  const double hdtdx = 0.5 * dt / dx;  // .5d0*dt/dx, half_step_extrapolation.f90:20
+  DevParams P = ctx->dp;
+  return elem_call(ctx, 2, in, isz, 2, out, osz, [&](char* base, const size_t* off) {
+    return launch_half_step(P, (const double*)(base + off[0]), (const double*)(base + off[1]), n, axis, hdtdx,
+                            (double*)(base + off[2]), (double*)(base + off[3]), ctx->stream);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,246 @@
+"""ctypes binding of librhyme_gpu.so, mirroring Rhyme's module interfaces.
+
+    ctx = Context(hydro_params(...))             # rhyme_*_init
+    box = ctx.register_box(cells)                # samr%levels(0)%boxes(1)
+    dt  = ctx.cfl_time_step(box, dx)             # rhyme_cfl_time_step
+    ctx.set_boundaries(box)                      # rhyme_samr_bc_set_boundaries
+    ctx.muscl_hancock_solve(box, dx, dt)         # rhyme_muscl_hancock_solve
+    ctx.sync_to_host(box)                        # cells now hold the new state
+
+`cells` is a C-ordered float64 numpy array of shape
+(NCMP, [N3+4,] [N2+4,] N1+4): the memory of the Fortran array
+cells(-1:N1+2, ..., 1:NCMP). There is no CPU fallback: if the library is
+missing or no GPU is present, calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "librhyme_gpu.so")
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ENANSTATE, ENOTFOUND = 0, -1, -2, -3, -4, -5, -6
+_NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMEDOUT",
+          ENANSTATE: "ENANSTATE", ENOTFOUND: "ENOTFOUND"}
+
+# Every symbol include/rhyme_gpu.h declares.
+EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rhyme_gpu_last_error",
+           "rhyme_gpu_get_stream", "rhyme_gpu_register_box", "rhyme_gpu_unregister_box",
+           "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step",
+           "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
+           "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
+           "rhyme_gpu_half_step"]
+
+
+class RhymeGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    """struct rhyme_gpu_params (include/rhyme_gpu.h)."""
+    _fields_ = [("ndim", C.c_int), ("limiter", C.c_int), ("n_iteration", C.c_int),
+                ("solver_type", C.c_int), ("bc", C.c_int * 6), ("precision", C.c_int),
+                ("reserved", C.c_int), ("gamma", C.c_double), ("kb_amu", C.c_double),
+                ("courant", C.c_double), ("omega", C.c_double), ("vacuum_density", C.c_double),
+                ("vacuum_pressure", C.c_double), ("tolerance", C.c_double),
+                ("inflow", (C.c_double * 5) * 6)]
+
+
+def params_struct(p):
+    s = Params()
+    s.ndim = p["ndim"]
+    s.limiter = p["limiter"]
+    s.n_iteration = p["n_iter"]
+    s.solver_type = p.get("solver_type", 2)
+    for i, b in enumerate(p["bc"]):
+        s.bc[i] = b
+    s.precision = p.get("precision", 0)
+    s.gamma = p["gamma"]
+    s.kb_amu = p["kb_amu"]
+    s.courant = p["courant"]
+    s.omega = p.get("omega", 0.0)
+    s.vacuum_density = p.get("vac_rho", 0.0)
+    s.vacuum_pressure = p.get("vac_p", 0.0)
+    s.tolerance = p["tol"]
+    inflow = p.get("inflow")
+    if inflow is not None:
+        for i in range(6):
+            for c in range(min(5, len(inflow[i]))):
+                s.inflow[i][c] = inflow[i][c]
+    return s
+
+
+_lib = None
+
+
+def load():
+    """Load librhyme_gpu.so (built by rhyme_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("librhyme_gpu.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    dp, ip, vp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
+    L.rhyme_gpu_abi_version.restype = C.c_int
+    L.rhyme_gpu_create.argtypes = [C.POINTER(vp), C.POINTER(Params)]
+    L.rhyme_gpu_destroy.argtypes = [vp]
+    L.rhyme_gpu_last_error.argtypes = [vp]
+    L.rhyme_gpu_last_error.restype = C.c_char_p
+    L.rhyme_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.rhyme_gpu_register_box.argtypes = [vp, C.c_int, C.c_int, dp, ip, C.c_int, C.c_int, ip]
+    L.rhyme_gpu_unregister_box.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_sync_to_device.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_sync_to_host.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_cfl_time_step.argtypes = [vp, C.c_int, dp, dp]
+    L.rhyme_gpu_set_boundaries.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_mh_solve.argtypes = [vp, C.c_int, dp, C.c_double]
+    L.rhyme_gpu_run.argtypes = [vp, C.c_int, dp, C.c_int, dp]
+    L.rhyme_gpu_synchronize.argtypes = [vp]
+    L.rhyme_gpu_riemann_solve.argtypes = [vp, dp, dp, C.c_longlong, C.c_double, C.c_double, C.c_int, dp]
+    L.rhyme_gpu_irs_exec.argtypes = [vp, dp, C.c_longlong, dp]
+    L.rhyme_gpu_slope_limiter.argtypes = [vp, dp, dp, dp, C.c_longlong, dp]
+    L.rhyme_gpu_half_step.argtypes = [vp, dp, dp, C.c_longlong, C.c_int, C.c_double, C.c_double, dp, dp]
+    _lib = L
+    return L
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _dx3(dx):
+    d = np.ones(3)
+    d[:len(dx)] = dx
+    return d
+
+
+class Box:
+    def __init__(self, ctx, handle, cells, dims):
+        self.ctx, self.handle, self.cells, self.dims = ctx, handle, cells, dims
+
+
+class Context:
+    """One rhyme_gpu_ctx: run parameters, a CUDA stream, registered boxes."""
+
+    def __init__(self, params):
+        self.lib = load()
+        self.params = dict(params)
+        self.ndim = int(params["ndim"])
+        self._p = params_struct(params)
+        h = C.c_void_p()
+        rc = self.lib.rhyme_gpu_create(C.byref(h), C.byref(self._p))
+        if rc != OK:
+            raise RhymeGpuError(rc, "rhyme_gpu_create failed (see stderr)")
+        self.h = h
+        self.boxes = []
+
+    def _check(self, rc):
+        if rc != OK:
+            raise RhymeGpuError(rc, self.lib.rhyme_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rhyme_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        s = C.c_void_p()
+        self._check(self.lib.rhyme_gpu_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    # ---- boxes ---------------------------------------------------------
+    def register_box(self, cells, level=0, number=1):
+        assert cells.dtype == np.float64 and cells.flags.c_contiguous
+        D = self.ndim
+        ext = cells.shape[1:][::-1]
+        assert len(ext) == D, "cells must have NDIM spatial axes"
+        dims = np.ones(3, dtype=np.int32)
+        for a in range(D):
+            dims[a] = ext[a] - 4
+        handle = C.c_int()
+        self._check(self.lib.rhyme_gpu_register_box(self.h, level, number, _d(cells),
+                                                    dims.ctypes.data_as(C.POINTER(C.c_int)), 2,
+                                                    cells.shape[0], C.byref(handle)))
+        b = Box(self, handle.value, cells, dims)
+        self.boxes.append(b)
+        return b
+
+    def unregister_box(self, box):
+        self._check(self.lib.rhyme_gpu_unregister_box(self.h, box.handle))
+
+    def sync_to_device(self, box):
+        self._check(self.lib.rhyme_gpu_sync_to_device(self.h, box.handle))
+
+    def sync_to_host(self, box):
+        self._check(self.lib.rhyme_gpu_sync_to_host(self.h, box.handle))
+
+    def synchronize(self):
+        self._check(self.lib.rhyme_gpu_synchronize(self.h))
+
+    # ---- the driver's step ---------------------------------------------
+    def cfl_time_step(self, box, dx):
+        dt = C.c_double()
+        self._check(self.lib.rhyme_gpu_cfl_time_step(self.h, box.handle, _d(_dx3(dx)), C.byref(dt)))
+        return dt.value
+
+    def set_boundaries(self, box):
+        self._check(self.lib.rhyme_gpu_set_boundaries(self.h, box.handle))
+
+    def muscl_hancock_solve(self, box, dx, dt):
+        self._check(self.lib.rhyme_gpu_mh_solve(self.h, box.handle, _d(_dx3(dx)), float(dt)))
+
+    def run(self, box, dx, nsteps, trace=True):
+        """nsteps driver iterations on the device; returns the dt trace."""
+        dts = np.zeros(max(int(nsteps), 1)) if trace else None
+        self._check(self.lib.rhyme_gpu_run(self.h, box.handle, _d(_dx3(dx)), int(nsteps),
+                                           _d(dts) if trace else None))
+        return dts[:nsteps] if trace else None
+
+    # ---- element-level interfaces --------------------------------------
+    def riemann_problem_solve(self, l, r, dx, dt, axis):
+        l, r = _f64(l), _f64(r)
+        u = np.zeros_like(l)
+        self._check(self.lib.rhyme_gpu_riemann_solve(self.h, _d(l), _d(r), l.shape[0], float(dx),
+                                                     float(dt), int(axis), _d(u)))
+        return u
+
+    def irs_exec(self, states):
+        states = _f64(states)
+        out = np.zeros((states.shape[0], 3))
+        self._check(self.lib.rhyme_gpu_irs_exec(self.h, _d(states), states.shape[0], _d(out)))
+        return out
+
+    def slope_limiter_run(self, ul, u, ur):
+        ul, u, ur = _f64(ul), _f64(u), _f64(ur)
+        d = np.zeros_like(u)
+        self._check(self.lib.rhyme_gpu_slope_limiter(self.h, _d(ul), _d(u), _d(ur), u.shape[0], _d(d)))
+        return d
+
+    def half_step_extrapolation(self, u, delta, axis, dx, dt):
+        u, delta = _f64(u), _f64(delta)
+        l = np.zeros_like(u)
+        r = np.zeros_like(u)
+        self._check(self.lib.rhyme_gpu_half_step(self.h, _d(u), _d(delta), u.shape[0], int(axis),
+                                                 float(dx), float(dt), _d(l), _d(r)))
+        return l, r

@@ -1,0 +1,59 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol
+include/rhyme_gpu.h declares, its struct layout matches, and parameter
+validation rejects bad input before any CUDA call."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from rhyme_gb300 import build, gpu, params
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return gpu.load()
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "rhyme_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(rhyme_gpu_\w+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = header_symbols()
+    assert len(declared) >= 17
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(gpu.EXPORTS) == declared
+
+
+def test_abi_version(lib):
+    assert lib.rhyme_gpu_abi_version() == 1
+
+
+def test_params_layout():
+    # 10 ints (incl. bc[6]) + precision + reserved = 12 ints, then 7 doubles, then 30 doubles
+    assert C.sizeof(gpu.Params) == 12 * 4 + 7 * 8 + 30 * 8
+    assert gpu.Params.gamma.offset == 48
+
+
+@pytest.mark.parametrize("bad", [dict(ndim=4), dict(limiter=9), dict(solver_type=3), dict(gamma=1.0),
+                                 dict(bc=[7, 2, 2, 2, 2, 2]), dict(precision=5), dict(n_iter=-1)])
+def test_create_rejects_bad_params(lib, bad):
+    p = params.hydro_params(2)
+    p.update(bad)
+    s = gpu.params_struct(p)
+    h = C.c_void_p()
+    rc = lib.rhyme_gpu_create(C.byref(h), C.byref(s))
+    assert rc == gpu.EINVAL
+    assert not h.value
+
+
+def test_null_arguments(lib):
+    assert lib.rhyme_gpu_create(None, None) == gpu.EINVAL
+    assert lib.rhyme_gpu_synchronize(None) == gpu.EINVAL
+    assert lib.rhyme_gpu_last_error(None) == b""
