@@ -117,8 +117,18 @@ int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle);
 /* Host -> device copy of the hydro components (and ghosts) of a box. */
 int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle);
 /* Device -> host copy into the registered cells array; waits for the stream
- * (bounded wait, RHYME_GPU_ETIMEDOUT). Checks the box's status word. */
+ * (bounded wait, RHYME_GPU_ETIMEDOUT). */
 int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle);
+
+/*
+ * Reads and clears the box's status word (no reference counterpart: the
+ * reference only logs, rhyme_sanity_check_perform.f90:34-63). Bit 0 is set
+ * when a CFL pass met a cell with non-positive density or a non-finite
+ * signal speed; such cells are skipped by the dt maximum exactly as the
+ * reference's `if (u > max_u)` skips them, and the run goes on. Returns
+ * RHYME_GPU_ENANSTATE when a bit is set, RHYME_GPU_OK otherwise.
+ */
+int rhyme_gpu_box_status(rhyme_gpu_ctx* ctx, int handle, int* flags);
 
 /*
  * dt = courant * minval(dx) / max(|v| + cs) over the box interior.
@@ -154,6 +164,16 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  */
 int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
                   int nsteps, double* dt_trace);
+
+/*
+ * Instrumentation (no reference counterpart): runs nsteps driver steps with
+ * direct launches and CUDA events between the library's kernels on the
+ * context stream; ms[5] receives the mean milliseconds per launch of the
+ * phases cfl, ghost_fill, faces, fluxes, update. The state advances nsteps
+ * steps exactly as rhyme_gpu_run would advance it.
+ */
+int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
+                            int nsteps, double ms[5]);
 
 /* Waits (bounded) for all work on the context stream. */
 int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);

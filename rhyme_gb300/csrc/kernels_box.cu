@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kUpdBlock)
 
 template <int D>
 cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const Geom& g,
-                       const Dx& dx, const StepScratch& s, cudaStream_t st) {
+                       const Dx& dx, const StepScratch& s, cudaStream_t st, cudaEvent_t* ev) {
   long long tot_f = 0, tot_r = 0;
   for (int a = 0; a < D; ++a) {
     long long f = 1, r = 1;
@@ -353,13 +353,17 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
     if (f > tot_f) tot_f = f;
     if (r > tot_r) tot_r = r;
   }
+  if (ev) cudaEventRecord(ev[0], st);
   dim3 gf(grid_for(tot_f, kFaceBlock), D);
   faces_kernel<D><<<gf, kFaceBlock, 0, st>>>(P, U, g, dx, s.dt, s.faces);
+  if (ev) cudaEventRecord(ev[1], st);
   dim3 gr(grid_for(tot_r, kFluxBlock), D);
   flux_kernel<D><<<gr, kFluxBlock, 0, st>>>(P, s.faces, g, s.fluxes);
+  if (ev) cudaEventRecord(ev[2], st);
   const long long tot_u = (long long)g.n[0] * g.n[1] * g.n[2];
   update_kernel<D><<<grid_for(tot_u, kUpdBlock), kUpdBlock, 0, st>>>(P, U, s.fluxes, g, dx, s.dt,
                                                                      Unew);
+  if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
 }
 
@@ -403,11 +407,11 @@ cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const
 }
 
 cudaError_t launch_mh_solve(const DevParams& P, const double* U, double* Unew, const Geom& g,
-                            const Dx& dx, const StepScratch& s, cudaStream_t st) {
+                            const Dx& dx, const StepScratch& s, cudaStream_t st, cudaEvent_t* ev) {
   switch (P.ndim) {
-    case 1: return mh_solve_d<1>(P, U, Unew, g, dx, s, st);
-    case 2: return mh_solve_d<2>(P, U, Unew, g, dx, s, st);
-    case 3: return mh_solve_d<3>(P, U, Unew, g, dx, s, st);
+    case 1: return mh_solve_d<1>(P, U, Unew, g, dx, s, st, ev);
+    case 2: return mh_solve_d<2>(P, U, Unew, g, dx, s, st, ev);
+    case 3: return mh_solve_d<3>(P, U, Unew, g, dx, s, st, ev);
   }
   return cudaErrorInvalidValue;
 }

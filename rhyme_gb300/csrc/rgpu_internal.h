@@ -72,8 +72,11 @@ cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, c
                               cudaStream_t st);
 cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const Dx& dx,
                        const StepScratch& s, cudaStream_t st);
+// ev (optional, 4 events): recorded before the face pass and after the face,
+// flux and update passes, for phase timing.
 cudaError_t launch_mh_solve(const DevParams& P, const double* U, double* Unew, const Geom& g,
-                            const Dx& dx, const StepScratch& s, cudaStream_t st);
+                            const Dx& dx, const StepScratch& s, cudaStream_t st,
+                            cudaEvent_t* ev = nullptr);
 int max_cfl_blocks();
 
 // Element-level launchers (kernels_elem.cu): device arrays in and out.

@@ -319,14 +319,23 @@ int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle) {
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return wait_stream(ctx);
+}
+
+int rhyme_gpu_box_status(rhyme_gpu_ctx* ctx, int handle, int* flags) {
+  if (!ctx || !flags) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   int* st = (int*)(ctx->pinned_dt + 1);
   CK(cudaMemcpyAsync(st, b->s.status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemsetAsync(b->s.status, 0, sizeof(int), ctx->stream));
   int rc = wait_stream(ctx);
   if (rc != RHYME_GPU_OK) return rc;
+  *flags = *st;
   if (*st & 1)
     return fail(ctx, RHYME_GPU_ENANSTATE,
-                "box (level %d, number %d) holds NaN/Inf or non-positive density", b->level, b->number);
+                "box (level %d, number %d) met non-positive density or a non-finite signal speed",
+                b->level, b->number);
   return RHYME_GPU_OK;
 }
 
@@ -566,3 +575,40 @@ int rhyme_gpu_half_step(rhyme_gpu_ctx* ctx, const double* u, const double* delta
 }
 
 }  // extern "C"
+
+extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int nsteps,
+                                       double ms[5]) {
+  if (!ctx || !dx || !ms || nsteps < 1) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  Dx d = make_dx(ctx->params.ndim, dx);
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
+  double acc[5] = {0, 0, 0, 0, 0};
+  int rc = RHYME_GPU_OK;
+  for (int s = 0; s < nsteps && rc == RHYME_GPU_OK; ++s) {
+    StepScratch sc = scratch_of(b, false);
+    double* U = b->state[b->cur];
+    double* V = b->state[1 - b->cur];
+    cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
+    if (e == cudaSuccess) e = launch_cfl(ctx->dp, U, b->g, d, sc, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+    if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
+    if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, d, sc, ctx->stream, ev + 2);
+    if (e != cudaSuccess) {
+      rc = fail(ctx, RHYME_GPU_ECUDA, "profile launch: %s", cudaGetErrorString(e));
+      break;
+    }
+    b->cur = 1 - b->cur;
+    rc = wait_stream(ctx);
+    if (rc != RHYME_GPU_OK) break;
+    for (int k = 0; k < 5; ++k) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      acc[k] += t;
+    }
+  }
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  for (int k = 0; k < 5; ++k) ms[k] = acc[k] / nsteps;
+  return rc;
+}

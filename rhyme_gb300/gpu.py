@@ -30,7 +30,8 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step",
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
-           "rhyme_gpu_half_step"]
+           "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status"]
+PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 
 
 class RhymeGpuError(RuntimeError):
@@ -104,6 +105,8 @@ def load():
     L.rhyme_gpu_irs_exec.argtypes = [vp, dp, C.c_longlong, dp]
     L.rhyme_gpu_slope_limiter.argtypes = [vp, dp, dp, dp, C.c_longlong, dp]
     L.rhyme_gpu_half_step.argtypes = [vp, dp, dp, C.c_longlong, C.c_int, C.c_double, C.c_double, dp, dp]
+    L.rhyme_gpu_profile_steps.argtypes = [vp, C.c_int, dp, C.c_int, dp]
+    L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     _lib = L
     return L
 
@@ -195,6 +198,14 @@ class Context:
     def sync_to_host(self, box):
         self._check(self.lib.rhyme_gpu_sync_to_host(self.h, box.handle))
 
+    def box_status(self, box):
+        """Status bits of the box since the last query (0 = clean)."""
+        f = C.c_int()
+        rc = self.lib.rhyme_gpu_box_status(self.h, box.handle, C.byref(f))
+        if rc not in (OK, ENANSTATE):
+            self._check(rc)
+        return f.value
+
     def synchronize(self):
         self._check(self.lib.rhyme_gpu_synchronize(self.h))
 
@@ -216,6 +227,12 @@ class Context:
         self._check(self.lib.rhyme_gpu_run(self.h, box.handle, _d(_dx3(dx)), int(nsteps),
                                            _d(dts) if trace else None))
         return dts[:nsteps] if trace else None
+
+    def profile_steps(self, box, dx, nsteps):
+        """Mean ms per launch of each phase (PHASES) over nsteps steps."""
+        ms = np.zeros(5)
+        self._check(self.lib.rhyme_gpu_profile_steps(self.h, box.handle, _d(_dx3(dx)), int(nsteps), _d(ms)))
+        return dict(zip(PHASES, ms.tolist()))
 
     # ---- element-level interfaces --------------------------------------
     def riemann_problem_solve(self, l, r, dx, dt, axis):

@@ -220,6 +220,23 @@ def test_vacuum_and_inflow():
     assert_fp64_parity(got, ref, ndim, dts, dts_ref)
 
 
+def test_status_word_reports_bad_cells():
+    """A cell with negative pressure (NaN sound speed) is skipped by the dt
+    maximum as in the reference, and reported through the status word."""
+    p = hydro_params(1, limiter=2, bc=[2] * 6)
+    cells = _random_box(1, [16], seed=1)
+    cells[2, 8] = -1.0  # negative total energy -> negative pressure
+    ref = cells.copy()
+    dt_ref = oracle.cfl_time_step(p, ref, [0.1])
+    with ctx_for(p) as ctx:
+        box = ctx.register_box(cells)
+        assert ctx.box_status(box) == 0
+        dt = ctx.cfl_time_step(box, [0.1])
+        assert ctx.box_status(box) == 1
+        assert ctx.box_status(box) == 0
+    assert dt == dt_ref
+
+
 def test_ghost_fill_and_cfl_direct():
     ndim, dims = 3, [9, 8, 7]
     p = hydro_params(ndim, bc=[1, 3, 2, 1, 3, 2])
