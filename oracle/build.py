@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "oracle_capi.cpp")]
-DEPS = SOURCES + [os.path.join(HERE, "rhyme_oracle.hpp")]
+DEPS = SOURCES + [os.path.join(HERE, "rhyme_oracle.hpp"),
+                  os.path.join(os.path.dirname(HERE), "rhyme_gb300", "csrc", "detmath.h")]
 
 
 def needs_build():

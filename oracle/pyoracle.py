@@ -12,7 +12,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["OracleParams", "params_struct", "lib", "run", "cfl_time_step",
+__all__ = ["set_pow_mode", "pow_mode", "pow_pair", "OracleParams", "params_struct", "lib", "run", "cfl_time_step",
            "set_boundaries", "mh_solve", "riemann_solve", "irs_exec",
            "guess_p_star", "nonlinear_wave", "star_and_sample",
            "slope_limiter", "half_step", "eos"]
@@ -76,8 +76,45 @@ def lib():
         L.oracle_slope_limiter.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp, dp, C.c_longlong, dp]
         L.oracle_half_step.argtypes = [C.c_int, C.c_double, dp, dp, C.c_longlong, C.c_int, C.c_double, C.c_double, dp, dp]
         L.oracle_eos.argtypes = [C.c_int, C.c_double, C.c_double, dp, C.c_longlong, C.c_int, dp, dp, dp]
+        L.oracle_set_pow_mode.argtypes = [C.c_int]
+        L.oracle_pow_pair.argtypes = [dp, dp, C.c_longlong, dp, dp]
         _lib = L
     return _lib
+
+
+def set_pow_mode(mode):
+    """0: C library pow (as the compiled reference); 1: det_pow (bit-exact
+    with the CUDA library). Returns the previous mode."""
+    global _pow_mode
+    prev = _pow_mode
+    if lib().oracle_set_pow_mode(int(mode)) != 0:
+        raise ValueError(mode)
+    _pow_mode = int(mode)
+    return prev
+
+
+_pow_mode = 0
+
+
+class pow_mode:
+    """Context manager selecting the oracle's power function."""
+
+    def __init__(self, mode):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = set_pow_mode(self.mode)
+
+    def __exit__(self, *a):
+        set_pow_mode(self.prev)
+
+
+def pow_pair(x, y):
+    x, y = _f64(x), _f64(y)
+    det = np.zeros_like(x)
+    libv = np.zeros_like(x)
+    lib().oracle_pow_pair(_d(x), _d(y), x.size, _d(det), _d(libv))
+    return det, libv
 
 
 def _d(a):

@@ -29,7 +29,22 @@
 #include <cstring>
 #include <vector>
 
+#include "../rhyme_gb300/csrc/detmath.h"
+
 namespace rhyme_oracle {
+
+// Power function used for every real `**` of the reference. Mode 0 is the C
+// library's pow, as the compiled Fortran calls it; mode 1 is
+// detmath::det_pow, the deterministic power function the CUDA library uses
+// (within one ulp of the C library's, see tests/test_oracle_golden.py), so
+// the GPU can be checked bit for bit.
+inline int& pow_mode() {
+  static int mode = 0;
+  return mode;
+}
+inline double opow(double x, double y) {
+  return pow_mode() == 1 ? detmath::det_pow(x, y) : std::pow(x, y);
+}
 
 // tiny(0d0) in Fortran is the smallest positive normal double.
 constexpr double kTiny = DBL_MIN;
@@ -233,8 +248,8 @@ inline void nonlinear_wave(const Gas& G, double s_rho, double s_p,
     f = (p - s_p) * factor;
     fprime = factor * (1.0 - (p - s_p) / (2.0 * (Bk + p)));
   } else {
-    f = 2.0 * s_cs / G.gm1 * (std::pow(p / s_p, G.gm1_2g) - 1.0);
-    fprime = 1.0 / (s_rho * s_cs) * std::pow(p / s_p, -G.gp1_2g);
+    f = 2.0 * s_cs / G.gm1 * (opow(p / s_p, G.gm1_2g) - 1.0);
+    fprime = 1.0 / (s_rho * s_cs) * opow(p / s_p, -G.gp1_2g);
   }
 }
 
@@ -259,13 +274,13 @@ inline void guess_p_star(const Gas& G, double l_rho, double vl, double l_p,
     ps[0] = ppv;  // PVRS
   } else if (ppv < p_min) {
     // Two-rarefaction
-    double pq = std::pow(l_p / r_p, G.gm1_2g);
+    double pq = opow(l_p / r_p, G.gm1_2g);
     double um = (pq * vl / l_cs + vr / r_cs + 2.0 / G.gm1 * (pq - 1.0)) /
                 (pq / l_cs + 1.0 / r_cs);
     double ptl = 1.0 + G.gm1 / 2.0 * (vl - um) / l_cs;
     double ptr = 1.0 + G.gm1 / 2.0 * (um - vr) / r_cs;
-    ps[0] = 0.5 * (l_p * std::pow(ptl, 1.0 / G.gm1_2g) +
-                   r_p * std::pow(ptr, 1.0 / G.gm1_2g));
+    ps[0] = 0.5 * (l_p * opow(ptl, 1.0 / G.gm1_2g) +
+                   r_p * opow(ptr, 1.0 / G.gm1_2g));
   } else {
     // Two-shock
     double gel = std::sqrt(((2.0 / (G.gp1)) / l_rho) / (G.gm1_gp1 * l_p + ppv));
@@ -279,9 +294,9 @@ inline void guess_p_star(const Gas& G, double l_rho, double vl, double l_p,
           (r_rho * r_cs + l_rho * l_cs);
 
   // Two-rarefaction approximation
-  ps[2] = std::pow((l_cs + r_cs - 0.5 * G.gm1 * (vr - vl)) /
-                       (std::pow(l_cs / l_p, G.gm1_2g) +
-                        std::pow(r_cs / r_p, G.gm1_2g)),
+  ps[2] = opow((l_cs + r_cs - 0.5 * G.gm1 * (vr - vl)) /
+                       (opow(l_cs / l_p, G.gm1_2g) +
+                        opow(r_cs / r_p, G.gm1_2g)),
                    1.0 / G.gm1_2g);
 
   // Two-shock approximation
@@ -372,8 +387,8 @@ inline void rp_star(const Gas& G, double vac_p, double tol, int n_iter,
         s.left.v[axis] - s.left.cs * std::sqrt(G.gp1_2g * ps_pl + G.gm1_2g);
   } else {
     s.sl.is_shock = false;
-    s.sl.fan_rho = s.left.rho * std::pow(ps_pl, G.g_inv);
-    s.sl.fan_cs = s.left.cs * std::pow(ps_pl, G.gm1_2g);
+    s.sl.fan_rho = s.left.rho * opow(ps_pl, G.g_inv);
+    s.sl.fan_cs = s.left.cs * opow(ps_pl, G.gm1_2g);
     s.sl.fan_speedH = s.left.v[axis] - s.left.cs;
     s.sl.fan_speedT = s.star_u - s.sl.fan_cs;
   }
@@ -386,8 +401,8 @@ inline void rp_star(const Gas& G, double vac_p, double tol, int n_iter,
         s.right.v[axis] + s.right.cs * std::sqrt(G.gp1_2g * ps_pr + G.gm1_2g);
   } else {
     s.sr.is_shock = false;
-    s.sr.fan_rho = s.right.rho * std::pow(ps_pr, G.g_inv);
-    s.sr.fan_cs = s.right.cs * std::pow(ps_pr, G.gm1_2g);
+    s.sr.fan_rho = s.right.rho * opow(ps_pr, G.g_inv);
+    s.sr.fan_cs = s.right.cs * opow(ps_pr, G.gm1_2g);
     s.sr.fan_speedH = s.right.v[axis] + s.right.cs;
     s.sr.fan_speedT = s.star_u + s.sr.fan_cs;
   }
@@ -398,12 +413,12 @@ template <int D>
 inline void w_kfan(const Gas& G, const Side<D>& s, double dxdt, int axis,
                    bool is_right, double* u) {
   double cs = is_right ? -s.cs : s.cs;
-  double rho = s.rho * std::pow(2.0 / G.gp1 + G.gm1_gp1 / cs * (s.v[axis] - dxdt),
+  double rho = s.rho * opow(2.0 / G.gp1 + G.gm1_gp1 / cs * (s.v[axis] - dxdt),
                                 2.0 / G.gm1);
   double v[D];
   for (int a = 0; a < D; ++a) v[a] = s.v[a];
   v[axis] = 2.0 / G.gp1 * (cs + G.gm1 / 2.0 * s.v[axis] + dxdt);
-  double p = s.p * std::pow(2.0 / G.gp1 + G.gm1_gp1 / cs * (s.v[axis] - dxdt),
+  double p = s.p * opow(2.0 / G.gp1 + G.gm1_gp1 / cs * (s.v[axis] - dxdt),
                             1.0 / G.gm1_2g);
   prim_vars_to_cons<D>(G, rho, v, p, u);
 }

@@ -26,7 +26,7 @@ UNITS = {
     "kernels_elem.cu": ["--fmad=false"],
     "rhyme_gpu.cu": ["--fmad=false"],
 }
-HEADERS = ["hydro.cuh", "rgpu_internal.h"]
+HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h"]
 
 
 def nvcc():

@@ -18,13 +18,26 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "detmath.h"
+
 namespace rgpu {
 
 // ---- math by type --------------------------------------------------------
+// Double powers go through detmath::det_pow, which the CPU oracle can run
+// bit for bit, so the FP64 path and its checker agree exactly even in flows
+// that amplify a one-ulp difference.
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
-__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ double m_pow(double x, double y) { return detmath::det_pow(x, y); }
 __device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+// x**y1 and x**y2 of one base (one logarithm for doubles).
+__device__ __forceinline__ void m_pow2(double x, double y1, double y2, double& r1, double& r2) {
+  detmath::det_pow2(x, y1, y2, &r1, &r2);
+}
+__device__ __forceinline__ void m_pow2(float x, float y1, float y2, float& r1, float& r2) {
+  r1 = powf(x, y1);
+  r2 = powf(x, y2);
+}
 __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
 
@@ -186,19 +199,42 @@ __device__ __forceinline__ void face_states(const Gas<T>& G, int lim, T w, const
 
 // ---- exact Riemann solver: rhyme_irs_*, rhyme_riemann_problem_* -----------
 
+// Loop-invariant terms of rhyme_irs_nonlinear_wave_function.f90:15-23 for one
+// side (Ak, Bk, 2cs/gm1, 1/(rho cs)): the reference recomputes them every
+// Newton iteration with the same operations, so computing them once gives the
+// same values.
+template <typename T>
+struct WaveSide {
+  T rho, p, cs, Ak, Bk, c2g, irc;
+};
+
+template <typename T>
+__device__ __forceinline__ WaveSide<T> wave_side(const Gas<T>& G, T s_rho, T s_p, T s_cs) {
+  WaveSide<T> w;
+  w.rho = s_rho;
+  w.p = s_p;
+  w.cs = s_cs;
+  w.Ak = T(2) / (G.gp1 * s_rho);
+  w.Bk = G.gm1 * s_p / G.gp1;
+  w.c2g = T(2) * s_cs / G.gm1;
+  w.irc = T(1) / (s_rho * s_cs);
+  return w;
+}
+
 // rhyme_irs_nonlinear_wave_function.f90:13-24
 template <typename T>
-__device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, T s_rho, T s_p, T s_cs, T p, T& f,
+__device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, const WaveSide<T>& w, T p, T& f,
                                                T& fprime) {
-  if (p > s_p) {
-    T Ak = T(2) / (G.gp1 * s_rho);
-    T Bk = G.gm1 * s_p / G.gp1;
-    T factor = m_sqrt(Ak / (Bk + p));
-    f = (p - s_p) * factor;
-    fprime = factor * (T(1) - (p - s_p) / (T(2) * (Bk + p)));
+  if (p > w.p) {
+    const T bp = w.Bk + p;
+    const T factor = m_sqrt(w.Ak / bp);
+    f = (p - w.p) * factor;
+    fprime = factor * (T(1) - (p - w.p) / (T(2) * bp));
   } else {
-    f = T(2) * s_cs / G.gm1 * (m_pow(p / s_p, G.gm1_2g) - T(1));
-    fprime = T(1) / (s_rho * s_cs) * m_pow(p / s_p, -G.gp1_2g);
+    T y, z;
+    m_pow2(p / w.p, G.gm1_2g, -G.gp1_2g, y, z);
+    f = w.c2g * (y - T(1));
+    fprime = w.irc * z;
   }
 }
 
@@ -252,12 +288,14 @@ template <typename T>
 __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
                                       T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f) {
   T p_star = T(0), p_prev, l_fp, r_fp;
+  const WaveSide<T> WL = wave_side(G, l_rho, l_p, l_cs);
+  const WaveSide<T> WR = wave_side(G, r_rho, r_p, r_cs);
   for (int gid = 0; gid < 6; ++gid) {
     p_star = guess_p_star(G, gid, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
     p_prev = p_star;
     for (int i = 1; i <= n_iter; ++i) {
-      nonlinear_wave(G, l_rho, l_p, l_cs, p_star, l_f, l_fp);
-      nonlinear_wave(G, r_rho, r_p, r_cs, p_star, r_f, r_fp);
+      nonlinear_wave(G, WL, p_star, l_f, l_fp);
+      nonlinear_wave(G, WR, p_star, r_f, r_fp);
       p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
       if (p_star < T(0)) break;
       if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) break;
@@ -301,8 +339,10 @@ __device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const 
     s.l_speed = L.v[AX] - L.cs * m_sqrt(G.gp1_2g * ps_pl + G.gm1_2g);
   } else {
     s.l_shock = false;
-    s.l_rho = L.rho * m_pow(ps_pl, G.g_inv);
-    s.l_cs = L.cs * m_pow(ps_pl, G.gm1_2g);
+    T pg, pa;
+    m_pow2(ps_pl, G.g_inv, G.gm1_2g, pg, pa);
+    s.l_rho = L.rho * pg;
+    s.l_cs = L.cs * pa;
     s.l_speedH = L.v[AX] - L.cs;
     s.l_speedT = s.u - s.l_cs;
   }
@@ -312,8 +352,10 @@ __device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const 
     s.r_speed = R.v[AX] + R.cs * m_sqrt(G.gp1_2g * ps_pr + G.gm1_2g);
   } else {
     s.r_shock = false;
-    s.r_rho = R.rho * m_pow(ps_pr, G.g_inv);
-    s.r_cs = R.cs * m_pow(ps_pr, G.gm1_2g);
+    T pg, pa;
+    m_pow2(ps_pr, G.g_inv, G.gm1_2g, pg, pa);
+    s.r_rho = R.rho * pg;
+    s.r_cs = R.cs * pa;
     s.r_speedH = R.v[AX] + R.cs;
     s.r_speedT = s.u + s.r_cs;
   }
@@ -323,12 +365,15 @@ __device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const 
 template <int D, int AX, typename T>
 __device__ __noinline__ void w_kfan(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
   T cs = is_right ? -s.cs : s.cs;
-  T rho = s.rho * m_pow(G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt), G.two_gm1);
+  const T base = G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt);
+  T prho, pp;
+  m_pow2(base, G.two_gm1, G.inv_gm1_2g, prho, pp);
+  T rho = s.rho * prho;
   T v[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) v[a] = s.v[a];
   v[AX] = G.two_gp1 * (cs + G.half_gm1 * s.v[AX] + dxdt);
-  T p = s.p * m_pow(G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt), G.inv_gm1_2g);
+  T p = s.p * pp;
   prim_vars_to_cons<D>(G, rho, v, p, u);
 }
 

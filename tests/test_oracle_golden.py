@@ -210,3 +210,38 @@ def test_guess_p_star_positive_and_wave_monotone(golden_dir):
     f = oracle.nonlinear_wave(g, rows4)
     assert np.all(np.diff(f[:, 0]) > 0.0)
     assert np.all(f[:, 1] > 0.0)
+
+
+def test_det_pow_within_one_ulp_of_libm():
+    """det_pow (the power function the CUDA path and the oracle's det mode
+    share) is within one ulp of the C library's pow over 12 decades of the
+    base and the exponents the hydro path uses."""
+    rng = np.random.default_rng(0)
+    x = np.exp(rng.uniform(-28, 28, 400000)) * rng.uniform(0.5, 1.5, 400000)
+    out = []
+    for g in GAMMA.values():
+        gm1, gp1 = g - 1.0, g + 1.0
+        for y in (gm1 / (2 * g), -gp1 / (2 * g), 1.0 / g, 2.0 / gm1, 1.0 / (gm1 / (2 * g))):
+            det, libv = oracle.pow_pair(x, np.full_like(x, y))
+            ulp = np.abs(det.view(np.int64) - libv.view(np.int64))
+            assert ulp.max() <= 1, (g, y, ulp.max())
+            out.append(np.mean(ulp != 0))
+    assert max(out) < 0.05
+    # special values
+    det, libv = oracle.pow_pair(np.array([0.0, 1.0, 4.0, 1e-310, -8.0]), np.array([0.2, 0.3, 0.5, 0.2, 3.0]))
+    assert np.array_equal(det, libv)
+
+
+def test_det_mode_matches_libm_mode_closely(golden_dir):
+    """The oracle's det_pow mode passes the same golden p* rows and stays
+    within 1e-13 of the libm mode."""
+    rows = load_p_stars(golden_dir)
+    g_single = float(np.float32(5.0) / np.float32(3.0))
+    l_rho, l_v, l_p, r_rho, r_v, r_p, exp = rows.T
+    states = np.stack([l_rho, l_v, l_p, np.sqrt(g_single * l_p / l_rho), r_rho, r_v, r_p,
+                       np.sqrt(g_single * r_p / r_rho)], axis=1)
+    a = oracle.irs_exec(GAMMA["monatomic"], 1e-10, 100000, states)
+    with oracle.pow_mode(1):
+        b = oracle.irs_exec(GAMMA["monatomic"], 1e-10, 100000, states)
+    assert all(within(b[i, 0], exp[i], 6) for i in range(1000))
+    np.testing.assert_allclose(b, a, rtol=1e-13)
