@@ -54,7 +54,9 @@ enum { RHYME_GPU_REFLECTIVE = 1, RHYME_GPU_OUTFLOW = 2, RHYME_GPU_PERIODIC = 3,
        RHYME_GPU_INFLOW = 4 };
 /* Solver ids: mhid, rhyme_muscl_hancock.f90:10-15. */
 enum { RHYME_GPU_CPU_INTENSIVE = 1, RHYME_GPU_MEMORY_INTENSIVE = 2 };
-/* Arithmetic of the step (this library). */
+/* Arithmetic of the step (this library): FP64 throughout, or FP32
+ * reconstruction / Riemann / flux with FP64 state accumulation and an FP64
+ * Riemann fallback near vacuum or where the FP32 Newton iteration fails. */
 enum { RHYME_GPU_FP64 = 0, RHYME_GPU_MIXED = 1 };
 
 /*
@@ -174,6 +176,13 @@ int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  */
 int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
                             int nsteps, double ms[5]);
+
+/*
+ * Instrumentation (no reference counterpart): number of interfaces of the
+ * box that the mixed-precision solver redid with the FP64 Riemann solver
+ * since the last query (0 in FP64 mode); clears the counter.
+ */
+int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count);
 
 /* Waits (bounded) for all work on the context stream. */
 int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);

@@ -25,6 +25,7 @@ UNITS = {
     "kernels_box.cu": ["--fmad=false"],
     "kernels_elem.cu": ["--fmad=false"],
     "rhyme_gpu.cu": ["--fmad=false"],
+    "kernels_mixed.cu": [],
 }
 HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h"]
 

@@ -283,11 +283,15 @@ __device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T 
 }
 
 // rhyme_irs_exec.f90:19-44 with lazily evaluated guesses. l_f / r_f are the
-// wave functions at the last iterate before the final update.
+// wave functions at the last iterate before the final update. `converged`
+// (optional) tells whether the first guess met the tolerance within the
+// iteration cap.
 template <typename T>
 __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
-                                      T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f) {
+                                      T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f,
+                                      bool* converged = nullptr) {
   T p_star = T(0), p_prev, l_fp, r_fp;
+  if (converged) *converged = false;
   const WaveSide<T> WL = wave_side(G, l_rho, l_p, l_cs);
   const WaveSide<T> WR = wave_side(G, r_rho, r_p, r_cs);
   for (int gid = 0; gid < 6; ++gid) {
@@ -298,7 +302,10 @@ __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rh
       nonlinear_wave(G, WR, p_star, r_f, r_fp);
       p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
       if (p_star < T(0)) break;
-      if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) break;
+      if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) {
+        if (converged && gid == 0) *converged = true;
+        break;
+      }
       p_prev = p_star;
     }
     if (p_star > T(0)) break;
@@ -321,6 +328,7 @@ struct Star {
   T l_rho, l_speed, l_cs, l_speedH, l_speedT;  // speed = shock speed
   T r_rho, r_speed, r_cs, r_speedH, r_speedT;
   T l_f, r_f;
+  bool converged;  // first guess met the tolerance
 };
 
 // rhyme_riemann_problem_star.f90:12-65
@@ -328,7 +336,7 @@ template <int D, int AX, typename T>
 __device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
                                         const Side<D, T>& R, Star<T>& s) {
   s.p = irs_exec(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
-                 s.r_f);
+                 s.r_f, &s.converged);
   if (s.p < rp.vac_p) s.p = rp.vac_p;
   s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
   T ps_pl = s.p / L.p;
@@ -423,9 +431,13 @@ __device__ __forceinline__ void vacuum_state(const Gas<T>& G, const Rp<T>& rp, T
 }
 
 // rhyme_riemann_problem_solve.f90:17-103 sampled at x/t = dxdt.
-template <int D, int AX, typename T>
+// With CHECK, *need64 is set when the interface should be redone in double:
+// a vacuum or vacuum-generation branch, an interface within 10% of vacuum
+// generation or with a density or pressure ratio beyond 1e6, a first guess
+// whose Newton iteration missed the tolerance, or a non-finite state.
+template <int D, int AX, typename T, bool CHECK = false>
 __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
-                                         T dxdt, T* u) {
+                                         T dxdt, T* u, bool* need64 = nullptr) {
   Side<D, T> L, R;
   L.rho = fmax_ref(l[0], rp.vac_rho);
   R.rho = fmax_ref(r[0], rp.vac_rho);
@@ -434,6 +446,10 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
   const bool vacuum_left = L.rho < e_rho && R.rho > e_rho;
   const bool vacuum_both = L.rho < e_rho && R.rho < e_rho;
   const T tiny = Limits<T>::tiny();
+  if (CHECK && (vacuum_right || vacuum_left || vacuum_both)) {
+    *need64 = true;
+    return;
+  }
 
   if (vacuum_right) {
 #pragma unroll
@@ -476,6 +492,14 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
     T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
     T du = R.v[AX] - L.v[AX];
     T du_crit = T(2) * (L.cs + R.cs) / G.gm1;
+    if (CHECK) {
+      const T rmin = fmin_ref(L.rho, R.rho), rmax = fmax_ref(L.rho, R.rho);
+      const T pmin = fmin_ref(L.p, R.p), pmax = fmax_ref(L.p, R.p);
+      if (!(du_crit - du > T(0.1) * du_crit) || !(rmin * T(1e6) > rmax) || !(pmin * T(1e6) > pmax)) {
+        *need64 = true;
+        return;
+      }
+    }
     if (du_crit < du) {  // vacuum generation
       if (dxdt > s_starr) {
         if (dxdt > R.v[AX] + R.cs) prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
@@ -489,6 +513,10 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
     } else {
       Star<T> s;
       rp_star<D, AX>(G, rp, L, R, s);
+      if (CHECK && !s.converged) {
+        *need64 = true;
+        return;
+      }
       rp_sampling<D, AX>(G, L, R, s, dxdt, u);
     }
   }

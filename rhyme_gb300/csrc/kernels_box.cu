@@ -43,9 +43,9 @@ inline int grid_for(long long total, int block) {
 // rhyme_samr_bc_set_boundaries.f90:9-20, writing U and (if given) the mirror
 // buffer, so both state buffers carry the ghost values the reference array
 // holds after the fill.
-template <int D>
+template <int D, typename T>
 __global__ void __launch_bounds__(kFillBlock)
-    ghost_fill_kernel(DevParams P, double* __restrict__ U, double* __restrict__ M, Geom g,
+    ghost_fill_kernel(DevParams P, T* __restrict__ U, T* __restrict__ M, Geom g,
                       long long off1, long long off2, long long total) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kFillBlock)
     const long long base = g.at(D, idx[0], idx[1], idx[2]);  // cell 0 of the line
     const long long sa = g.s[axis];
     const long long N = g.n[axis];
-    double* f = U + (long long)c * g.field;
+    T* f = U + (long long)c * g.field;
     for (int side = 0; side < 2; ++side) {
       const int type = P.bc[2 * axis + side];
       long long g0, g1, s0, s1;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kFillBlock)
         s1 = (type == 3) ? base + 2 * sa : base + (N - 1) * sa;
       }
       if (type == 4) {  // inflow
-        const double v = P.inflow[2 * axis + side][c];
+        const T v = (T)P.inflow[2 * axis + side][c];
         f[g0] = v;
         f[g1] = v;
       } else if (type >= 1 && type <= 3) {
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kFillBlock)
         continue;
       }
       if (M) {
-        double* m = M + (long long)c * g.field;
+        T* m = M + (long long)c * g.field;
         m[g0] = f[g0];
         m[g1] = f[g1];
       }
@@ -371,8 +371,8 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
 
 int max_cfl_blocks() { return kMaxBlocks; }
 
-cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,
-                              cudaStream_t st) {
+template <typename T>
+cudaError_t ghost_fill_any(const DevParams& P, T* U, T* U_mirror, const Geom& g, cudaStream_t st) {
   const int D = P.ndim;
   long long per_axis[3] = {0, 0, 0};
   for (int a = 0; a < D; ++a) {
@@ -384,12 +384,21 @@ cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, c
   const long long off1 = per_axis[0], off2 = off1 + per_axis[1], total = off2 + per_axis[2];
   const int grid = grid_for(total, kFillBlock);
   switch (D) {
-    case 1: ghost_fill_kernel<1><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
-    case 2: ghost_fill_kernel<2><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
-    case 3: ghost_fill_kernel<3><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
+    case 1: ghost_fill_kernel<1, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
+    case 2: ghost_fill_kernel<2, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
+    case 3: ghost_fill_kernel<3, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,
+                              cudaStream_t st) {
+  return ghost_fill_any<double>(P, U, U_mirror, g, st);
+}
+
+cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st) {
+  return ghost_fill_any<float>(P, Uf, nullptr, g, st);
 }
 
 cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const Dx& dx,

@@ -1,0 +1,353 @@
+// kernels_mixed.cu -- mixed-precision MUSCL-Hancock step.
+//
+// The conserved state stays FP64 in HBM (U) and is mirrored once per step as
+// FP32 (Uf). Each axis is one fused sweep kernel: a CTA stages a slab of
+// Uf (S cells along the sweep axis plus the 2-cell ghost/halo layer, for P
+// pencils) in shared memory with coalesced loads, computes FP32 limited
+// slopes and half-step face states for S+2 cells, solves the S+1 exact
+// Riemann problems of the slab in FP32 and forms the flux difference of its
+// S cells. The flux differences of the axes are summed in FP32 in the
+// reference's association ((X + Y) + Z), and the last sweep adds the sum to
+// U in FP64 and writes U^{n+1} and its FP32 mirror: one FP64 add per
+// conserved component and cell, since on GB300 even FP64 adds are scarce.
+//
+// Interfaces that near vacuum, or whose FP32 Newton iteration misses the
+// tolerance on its first guess, are queued per CTA in shared memory and
+// redone with the FP64 Riemann solver (same device code, double).
+//
+// The CFL maximum of the mixed path is taken in FP32 over Uf; dt itself is
+// formed in FP64.
+#include "rgpu_internal.h"
+
+namespace rgpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxBlocks = 152 * 32;
+
+inline int grid_for(long long total, int block) {
+  long long b = (total + block - 1) / block;
+  if (b < 1) b = 1;
+  if (b > kMaxBlocks) b = kMaxBlocks;
+  return (int)b;
+}
+
+// U (FP64) -> Uf (FP32) over whole component blocks (ghosts included).
+__global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restrict__ U,
+                                                          float* __restrict__ Uf, long long n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    Uf[t] = (float)U[t];
+}
+
+// FP32 signal-speed maximum over the interior of Uf; the last block forms
+// dt = courant * min(dx) / max in FP64 and resets the accumulators.
+template <int D>
+__global__ void __launch_bounds__(kThreads)
+    cfl_f32_kernel(MixedParams M, const float* __restrict__ Uf, Geom g, double courant, double mdx,
+                   StepScratch s) {
+  const long long n0 = g.n[0], n1 = g.n[1];
+  const long long total = n0 * n1 * (long long)g.n[2];
+  float m = 0.f;
+  int bad = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0) + 1;
+    const long long q = t / n0;
+    const int j = (int)(q % n1) + 1;
+    const int k = (int)(q / n1) + 1;
+    const long long o = g.at(D, i, j, k);
+    float u[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) u[c] = Uf[(long long)c * g.field + o];
+    float ss = 0.f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
+    const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
+    if (v > m) m = v;
+    if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float o = __shfl_down_sync(0xffffffffu, m, off);
+    if (o > m) m = o;
+    bad |= __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  __shared__ float sm[kThreads / 32];
+  __shared__ int sb[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sm[warp] = m;
+    sb[warp] = bad;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    m = (lane < kThreads / 32) ? sm[lane] : 0.f;
+    bad = (lane < kThreads / 32) ? sb[lane] : 0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float o = __shfl_down_sync(0xffffffffu, m, off);
+      if (o > m) m = o;
+      bad |= __shfl_down_sync(0xffffffffu, bad, off);
+    }
+    if (lane == 0) {
+      // non-negative floats order like their bit patterns
+      atomicMax(s.max_bits, (unsigned long long)__float_as_uint(m));
+      if (bad) atomicOr(s.status, 1);
+      __threadfence();
+      const unsigned int prev = atomicAdd(s.counter, 1u);
+      if (prev == gridDim.x - 1) {
+        __threadfence();
+        const float mu = __uint_as_float((unsigned int)atomicAdd(s.max_bits, 0ull));
+        const double dt = courant * mdx / (double)mu;
+        *s.dt = dt;
+        if (s.dt_trace) {
+          const int pos = *s.trace_pos;
+          if (pos >= 0 && pos < s.trace_cap) s.dt_trace[pos] = dt;
+          *s.trace_pos = pos + 1;
+        }
+        atomicExch(s.max_bits, 0ull);
+        atomicExch(s.counter, 0u);
+      }
+    }
+  }
+}
+
+// Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),
+// acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
+enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
+
+// Slab geometry of axis A: pencils run along B (x unless A is x).
+template <int D, int A>
+struct Axes {
+  static constexpr int B = (D == 1) ? 1 : (A == 0 ? 1 : 0);
+  static constexpr int C = (D == 3) ? 3 - A - B : 2;
+};
+
+// Shared-memory slab; index (la along A, lb along the pencils) is stored
+// with the x-fast index innermost so consecutive threads hit consecutive
+// banks in both orientations.
+template <int D, int S, int P>
+struct SweepSmem {
+  float u[D + 2][(S + 4) * P];   // FP32 state slab (ghost/halo layer included)
+  float ul[D + 2][(S + 2) * P];  // face states, left / right
+  float ur[D + 2][(S + 2) * P];
+  float f[D + 2][(S + 1) * P];   // interface fluxes
+  int nfb;                       // FP64 fallback queue
+  short fb[(S + 1) * P];
+};
+
+template <int D, int A, int S, int P, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
+                 Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
+                 double* __restrict__ Unew, float* __restrict__ Ufnew, int* __restrict__ fb_count) {
+  constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
+  __shared__ SweepSmem<D, S, P> sh;
+  const int NA = g.n[A];
+  const int NB = (B < D) ? g.n[B] : 1;
+  // tile origin: the fast grid axis runs along x
+  const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
+  const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
+  const int a0 = tA * S + 1;  // first interior cell of the slab along A
+  const int b0 = tB * P + 1;
+  const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
+  const long long F = g.field;
+  const double dt = *dtp;
+  const float dtdx = (float)(dt / dx.v[A]);
+  const float hdtdx = (float)(0.5 * dt / dx.v[A]);
+
+  auto offset = [&](int ga, int gb) -> long long {
+    int c3[3] = {1, 1, 1};
+    c3[A] = ga;
+    if (B < D) c3[B] = gb;
+    if (C < D) c3[C] = cC;
+    return g.at(D, c3[0], c3[1], c3[2]);
+  };
+  // thread item -> (la, lb), x-fast first; ix() the matching smem index
+  auto split = [&](int it, int na, int& la, int& lb) {
+    if (A == 0) {
+      la = it % na;
+      lb = it / na;
+    } else {
+      lb = it % P;
+      la = it / P;
+    }
+  };
+  auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
+
+  if (threadIdx.x == 0) sh.nfb = 0;
+  // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
+  for (int it = threadIdx.x; it < (S + 4) * P; it += kThreads) {
+    int la, lb;
+    split(it, S + 4, la, lb);
+    const int ga = a0 - 2 + la, gb = b0 + lb;
+    const bool ok = ga <= NA + 2 && gb <= NB;
+    const long long o = ok ? offset(ga, gb) : 0;
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) sh.u[c][ix(la, lb, S + 4)] = ok ? Uf[(long long)c * F + o] : 0.f;
+  }
+  __syncthreads();
+
+  // 2. face states of cells a0-1 .. min(a0+S, NA+1)
+  for (int it = threadIdx.x; it < (S + 2) * P; it += kThreads) {
+    int la, lb;
+    split(it, S + 2, la, lb);
+    if (a0 - 1 + la > NA + 1 || b0 + lb > NB) continue;
+    float um[D + 2], u0[D + 2], up[D + 2], l[D + 2], r[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      um[c] = sh.u[c][ix(la, lb, S + 4)];
+      u0[c] = sh.u[c][ix(la + 1, lb, S + 4)];
+      up[c] = sh.u[c][ix(la + 2, lb, S + 4)];
+    }
+    face_states<D, A>(M.G, M.limiter, M.omega, um, u0, up, hdtdx, l, r);
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      sh.ul[c][ix(la, lb, S + 2)] = l[c];
+      sh.ur[c][ix(la, lb, S + 2)] = r[c];
+    }
+  }
+  __syncthreads();
+
+  // 3. FP32 Riemann problems at interfaces (a0-1+li | a0+li), li in [0, S]
+  for (int it = threadIdx.x; it < (S + 1) * P; it += kThreads) {
+    int li, lb;
+    split(it, S + 1, li, lb);
+    if (a0 - 1 + li > NA || b0 + lb > NB) continue;
+    float l[D + 2], r[D + 2], u[D + 2], f[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      l[c] = sh.ur[c][ix(li, lb, S + 2)];
+      r[c] = sh.ul[c][ix(li + 1, lb, S + 2)];
+    }
+    bool need64 = false;
+    rp_solve<D, A, float, true>(M.G, M.rp, l, r, 0.f, u, &need64);
+    if (!need64) {
+      flux<D, A>(M.G, u, f);
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c)
+        if (!isfinite(f[c])) need64 = true;
+    }
+    if (need64) {
+      const int q = atomicAdd(&sh.nfb, 1);
+      sh.fb[q] = (short)it;
+    } else {
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = f[c];
+    }
+  }
+  __syncthreads();
+
+  // 3b. queued interfaces in FP64, one per thread
+  const int nfb = sh.nfb;
+  for (int q = threadIdx.x; q < nfb; q += kThreads) {
+    int li, lb;
+    split(sh.fb[q], S + 1, li, lb);
+    double l[D + 2], r[D + 2], f[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      l[c] = (double)sh.ur[c][ix(li, lb, S + 2)];
+      r[c] = (double)sh.ul[c][ix(li + 1, lb, S + 2)];
+    }
+    interface_flux<D, A>(M.G64, M.rp64, l, r, f);
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = (float)f[c];
+  }
+  if (fb_count && threadIdx.x == 0 && nfb > 0) atomicAdd(fb_count, nfb);
+  __syncthreads();
+
+  // 4. flux differences of cells a0 .. a0+S-1 and the accumulation
+  for (int it = threadIdx.x; it < S * P; it += kThreads) {
+    int lu, lb;
+    split(it, S, lu, lb);
+    const int ga = a0 + lu, gb = b0 + lb;
+    if (ga > NA || gb > NB) continue;
+    const long long o = offset(ga, gb);
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const float x = dtdx * (sh.f[c][ix(lu, lb, S + 1)] - sh.f[c][ix(lu + 1, lb, S + 1)]);
+      const long long oc = (long long)c * F + o;
+      if (MODE == FIRST) {
+        acc[oc] = x;
+      } else if (MODE == MID) {
+        acc[oc] = acc[oc] + x;
+      } else {
+        const float tot = (MODE == LAST) ? acc[oc] + x : x;
+        const double un = U[oc] + (double)tot;
+        Unew[oc] = un;
+        Ufnew[oc] = (float)un;
+      }
+    }
+  }
+}
+
+template <int D, int A, int S, int P, int MODE>
+cudaError_t launch_sweep(const MixedParams& M, const float* Uf, const double* U, const Geom& g,
+                         const Dx& dx, const double* dtp, float* acc, double* Unew, float* Ufnew,
+                         int* fb_count, cudaStream_t st) {
+  constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
+  const int NA = g.n[A];
+  const int NB = (B < D) ? g.n[B] : 1;
+  const int NC = (C < D) ? g.n[C] : 1;
+  dim3 grid;
+  if (A == 0) {
+    grid = dim3((NA + S - 1) / S, (NB + P - 1) / P, NC);
+  } else {
+    grid = dim3((NB + P - 1) / P, (NA + S - 1) / S, NC);
+  }
+  sweep_kernel<D, A, S, P, MODE><<<grid, kThreads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew,
+                                                            fb_count);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st) {
+  to_f32_kernel<<<grid_for(n, kThreads), kThreads, 0, st>>>(U, Uf, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& g, double courant,
+                             const Dx& dx, const StepScratch& s, cudaStream_t st) {
+  const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+  int grid = grid_for(total, kThreads);
+  if (grid > 152 * 4) grid = 152 * 4;
+  switch (M.ndim) {
+    case 1: cfl_f32_kernel<1><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
+    case 2: cfl_f32_kernel<2><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
+    case 3: cfl_f32_kernel<3><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
+                                  double* Unew, float* Ufnew, float* acc, const Geom& g,
+                                  const Dx& dx, const StepScratch& s, int* fb_count,
+                                  cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  switch (M.ndim) {
+    case 1:
+      e = launch_sweep<1, 0, 256, 1, ONLY>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      break;
+    case 2:
+      e = launch_sweep<2, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      if (e == cudaSuccess)
+        e = launch_sweep<2, 1, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      break;
+    case 3:
+      e = launch_sweep<3, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      if (e == cudaSuccess)
+        e = launch_sweep<3, 1, 16, 16, MID>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      if (e == cudaSuccess)
+        e = launch_sweep<3, 2, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return e;
+}
+
+}  // namespace rgpu

@@ -20,6 +20,19 @@ struct DevParams {
   double courant;
 };
 
+// Parameters of the mixed-precision kernels: FP32 copies of the gas and
+// Riemann constants (rounded from their FP64 values) plus the FP64 set for
+// the fallback solver.
+struct MixedParams {
+  Gas<float> G;
+  Rp<float> rp;
+  Gas<double> G64;
+  Rp<double> rp64;
+  int ndim;
+  int limiter;
+  float omega;
+};
+
 // Geometry of one box in the reference layout: component blocks of
 // `field` doubles, cell (i,j,k) (1-based interior, ghosts -1..N+2) at
 // (i+1)*s0 + (j+1)*s1 + (k+1)*s2 for the active axes.
@@ -78,6 +91,16 @@ cudaError_t launch_mh_solve(const DevParams& P, const double* U, double* Unew, c
                             const Dx& dx, const StepScratch& s, cudaStream_t st,
                             cudaEvent_t* ev = nullptr);
 int max_cfl_blocks();
+
+// Mixed-precision launchers (kernels_mixed.cu).
+cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st);
+cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& g, double courant,
+                             const Dx& dx, const StepScratch& s, cudaStream_t st);
+cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
+                                  double* Unew, float* Ufnew, float* acc, const Geom& g,
+                                  const Dx& dx, const StepScratch& s, int* fb_count,
+                                  cudaStream_t st);
+cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 
 // Element-level launchers (kernels_elem.cu): device arrays in and out.
 cudaError_t launch_riemann_solve(const DevParams& P, const double* l, const double* r, long long n,

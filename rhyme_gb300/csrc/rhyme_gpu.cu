@@ -32,6 +32,9 @@ struct Box {
   double* state[2] = {nullptr, nullptr};
   int cur = 0;
   StepScratch s{};
+  float* Uf[2] = {nullptr, nullptr};  // FP32 mirrors of the state (mixed mode)
+  float* acc = nullptr;               // FP32 flux-difference accumulator (mixed mode)
+  int* fb_count = nullptr;            // interfaces redone in FP64 (mixed mode)
   double* trace_buf = nullptr;
   int* trace_pos = nullptr;
   bool registered_host = false;
@@ -45,6 +48,8 @@ struct Box {
 struct rhyme_gpu_ctx {
   rhyme_gpu_params params{};
   DevParams dp{};
+  MixedParams mp{};
+  bool mixed = false;
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
@@ -163,12 +168,44 @@ void make_dev_params(const rhyme_gpu_params* p, DevParams* d) {
   d->courant = p->courant;
 }
 
+void make_mixed_params(const DevParams& d, MixedParams* m) {
+  memset(m, 0, sizeof(*m));
+  const Gas<double>& G = d.G;
+  Gas<float>& F = m->G;
+  F.g = (float)G.g;
+  F.gm1 = (float)G.gm1;
+  F.gp1 = (float)G.gp1;
+  F.gm1_gp1 = (float)G.gm1_gp1;
+  F.gm1_2g = (float)G.gm1_2g;
+  F.gp1_2g = (float)G.gp1_2g;
+  F.g_inv = (float)G.g_inv;
+  F.kb_amu = (float)G.kb_amu;
+  F.two_gp1 = (float)G.two_gp1;
+  F.two_gm1 = (float)G.two_gm1;
+  F.inv_gm1_2g = (float)G.inv_gm1_2g;
+  F.gm1_half = (float)G.gm1_half;
+  F.half_gm1 = (float)G.half_gm1;
+  F.g_kb_amu = (float)G.g_kb_amu;
+  m->rp.vac_rho = (float)d.rp.vac_rho;
+  m->rp.vac_p = (float)d.rp.vac_p;
+  m->rp.vac_rho_next = std::nextafter((float)d.rp.vac_rho, 1.0f);
+  m->rp.tol = (float)d.rp.tol;
+  m->rp.n_iter = d.rp.n_iter;
+  m->G64 = d.G;
+  m->rp64 = d.rp;
+  m->ndim = d.ndim;
+  m->limiter = d.limiter;
+  m->omega = (float)d.omega;
+}
+
 void destroy_box(Box* b) {
   if (!b) return;
   for (int i = 0; i < 2; ++i) {
     if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
     cudaFree(b->state[i]);
+    cudaFree(b->Uf[i]);
   }
+  cudaFree(b->acc);
   cudaFree(b->s.faces);
   cudaFree(b->s.fluxes);
   cudaFree(b->s.dt);
@@ -204,6 +241,8 @@ int rhyme_gpu_create(rhyme_gpu_ctx** out, const rhyme_gpu_params* params) {
   }
   ctx->params = *params;
   make_dev_params(params, &ctx->dp);
+  make_mixed_params(ctx->dp, &ctx->mp);
+  ctx->mixed = (params->precision == RHYME_GPU_MIXED);
   const char* to = getenv("RHYME_GPU_TIMEOUT_S");
   if (to && atof(to) > 0) ctx->timeout_s = atof(to);
   cudaError_t e = cudaGetDevice(&ctx->device);
@@ -264,8 +303,13 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   b->hydro_bytes = (size_t)(D + 2) * F * sizeof(double);
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->state[i], b->hydro_bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double));
+  if (ctx->mixed) {
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->Uf[i], (size_t)(D + 2) * F * sizeof(float));
+    if (e == cudaSuccess && D > 1) e = cudaMalloc(&b->acc, (size_t)(D + 2) * F * sizeof(float));
+  } else {
+    if (e == cudaSuccess) e = cudaMalloc(&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double));
+  }
   // small block: dt, max_bits, counter, status, trace_pos, then the trace
   const size_t small = 64 + sizeof(double) * kTraceCap;
   if (e == cudaSuccess) e = cudaMalloc(&b->s.dt, small);
@@ -280,6 +324,7 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   b->s.counter = (unsigned int*)(base + 16);
   b->s.status = (int*)(base + 20);
   b->trace_pos = (int*)(base + 24);
+  b->fb_count = (int*)(base + 28);
   b->trace_buf = (double*)(base + 64);
   // Pin the caller's array for asynchronous copies when possible; a failure
   // here only costs copy speed.
@@ -310,6 +355,11 @@ int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle) {
   CK(cudaMemcpyAsync(b->state[b->cur], b->host, b->hydro_bytes, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(b->state[1 - b->cur], b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToDevice,
                      ctx->stream));
+  if (ctx->mixed) {
+    const long long n = (long long)(ctx->params.ndim + 2) * b->g.field;
+    CK(launch_to_f32(b->state[b->cur], b->Uf[b->cur], n, ctx->stream));
+    CK(launch_to_f32(b->state[b->cur], b->Uf[1 - b->cur], n, ctx->stream));
+  }
   if (!b->registered_host) return wait_stream(ctx);
   return RHYME_GPU_OK;
 }
@@ -360,6 +410,15 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
   StepScratch s = scratch_of(b, trace);
   double* U = b->state[cur];
   double* V = b->state[1 - cur];
+  if (ctx->mixed) {
+    cudaError_t e = launch_cfl_mixed(ctx->mp, b->Uf[cur], b->g, ctx->dp.courant, dx, s, ctx->stream);
+    if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
+    if (e == cudaSuccess) e = launch_ghost_fill_f32(ctx->dp, b->Uf[cur], b->g, ctx->stream);
+    if (e == cudaSuccess)
+      e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fb_count,
+                                ctx->stream);
+    return e;
+  }
   cudaError_t e = launch_cfl(ctx->dp, U, b->g, dx, s, ctx->stream);
   if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
   if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, dx, s, ctx->stream);
@@ -402,7 +461,10 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], 
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   Dx d = make_dx(ctx->params.ndim, dx);
-  CK(launch_cfl(ctx->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
+  if (ctx->mixed)
+    CK(launch_cfl_mixed(ctx->mp, b->Uf[b->cur], b->g, ctx->dp.courant, d, scratch_of(b, false), ctx->stream));
+  else
+    CK(launch_cfl(ctx->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
   CK(cudaMemcpyAsync(ctx->pinned_dt, b->s.dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   int rc = wait_stream(ctx);
   if (rc != RHYME_GPU_OK) return rc;
@@ -415,6 +477,7 @@ int rhyme_gpu_set_boundaries(rhyme_gpu_ctx* ctx, int handle) {
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   CK(launch_ghost_fill(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, ctx->stream));
+  if (ctx->mixed) CK(launch_ghost_fill_f32(ctx->dp, b->Uf[b->cur], b->g, ctx->stream));
   return RHYME_GPU_OK;
 }
 
@@ -430,8 +493,12 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   if (rc != RHYME_GPU_OK) return rc;
   ctx->pinned_dt[0] = dt;
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_mh_solve(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
-                     ctx->stream));
+  if (ctx->mixed)
+    CK(launch_mh_solve_mixed(ctx->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
+                             b->acc, b->g, d, scratch_of(b, false), b->fb_count, ctx->stream));
+  else
+    CK(launch_mh_solve(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
+                       ctx->stream));
   b->cur = 1 - b->cur;
   return RHYME_GPU_OK;
 }
@@ -591,10 +658,25 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
     double* U = b->state[b->cur];
     double* V = b->state[1 - b->cur];
     cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
-    if (e == cudaSuccess) e = launch_cfl(ctx->dp, U, b->g, d, sc, ctx->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
-    if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
-    if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, d, sc, ctx->stream, ev + 2);
+    if (ctx->mixed) {
+      // mixed: the fused sweeps are reported under "fluxes"
+      if (e == cudaSuccess) e = launch_cfl_mixed(ctx->mp, b->Uf[b->cur], b->g, ctx->dp.courant, d, sc, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+      if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
+      if (e == cudaSuccess) e = launch_ghost_fill_f32(ctx->dp, b->Uf[b->cur], b->g, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[3], ctx->stream);
+      if (e == cudaSuccess)
+        e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
+                                  b->fb_count, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[4], ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[5], ctx->stream);
+    } else {
+      if (e == cudaSuccess) e = launch_cfl(ctx->dp, U, b->g, d, sc, ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+      if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
+      if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, d, sc, ctx->stream, ev + 2);
+    }
     if (e != cudaSuccess) {
       rc = fail(ctx, RHYME_GPU_ECUDA, "profile launch: %s", cudaGetErrorString(e));
       break;
@@ -611,4 +693,17 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 5; ++k) ms[k] = acc[k] / nsteps;
   return rc;
+}
+
+extern "C" int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count) {
+  if (!ctx || !count) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  int* st = (int*)(ctx->pinned_dt + 2);
+  CK(cudaMemcpyAsync(st, b->fb_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemsetAsync(b->fb_count, 0, sizeof(int), ctx->stream));
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  *count = *st;
+  return RHYME_GPU_OK;
 }

@@ -30,7 +30,8 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step",
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
-           "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status"]
+           "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
+           "rhyme_gpu_fallback_count"]
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 
 
@@ -107,6 +108,7 @@ def load():
     L.rhyme_gpu_half_step.argtypes = [vp, dp, dp, C.c_longlong, C.c_int, C.c_double, C.c_double, dp, dp]
     L.rhyme_gpu_profile_steps.argtypes = [vp, C.c_int, dp, C.c_int, dp]
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
+    L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -205,6 +207,12 @@ class Context:
         if rc not in (OK, ENANSTATE):
             self._check(rc)
         return f.value
+
+    def fallback_count(self, box):
+        """Interfaces redone in FP64 by the mixed solver since the last query."""
+        n = C.c_longlong()
+        self._check(self.lib.rhyme_gpu_fallback_count(self.h, box.handle, C.byref(n)))
+        return n.value
 
     def synchronize(self):
         self._check(self.lib.rhyme_gpu_synchronize(self.h))
