@@ -256,8 +256,8 @@ def run_gpu(args, rank, local, world):
     barrier(world)
     t_end = time.time()
     clk = clocks.stop(t_begin, t_end)
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    ms = allmax(ms, world)
+    per_step = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = allmax(sum(per_step), world)
     value = world * interior * K / (ms * 1e-3)
 
     # phase timing of the same step (direct launches, events between kernels)
@@ -301,7 +301,8 @@ def run_gpu(args, rank, local, world):
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
-                "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+                "warmup": W, "ms_per_step": ms / K, "ms_per_step_median": statistics.median(per_step),
+                "ms_per_step_max": max(per_step), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(cfg, l2="flushed (512 MiB write) between timed steps, outside the events",
                                parallelism="replicas" if world > 1 else "single box"),

@@ -141,6 +141,14 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
                             double* dt);
 
 /*
+ * The same time step returned as the function value (a negative value on
+ * error, message in rhyme_gpu_last_error), for Fortran callers that must
+ * call it from the pure rhyme_cfl_time_step (rhyme_cfl.f90:19-23): a pure
+ * Fortran function cannot take an intent(out) argument.
+ */
+double rhyme_gpu_cfl_dt(rhyme_gpu_ctx* ctx, int handle, const double dx[3]);
+
+/*
  * Ghost fill of the 2-cell face slabs (corners untouched) with the context's
  * boundary types. Replaces pure subroutine rhyme_samr_bc_set_boundaries
  * (rhyme_samr_bc.f90:38-41, rhyme_samr_bc_set_boundaries.f90:9-20).

@@ -472,6 +472,12 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], 
   return RHYME_GPU_OK;
 }
 
+double rhyme_gpu_cfl_dt(rhyme_gpu_ctx* ctx, int handle, const double dx[3]) {
+  double dt = -1.0;
+  if (rhyme_gpu_cfl_time_step(ctx, handle, dx, &dt) != RHYME_GPU_OK) return -1.0;
+  return dt;
+}
+
 int rhyme_gpu_set_boundaries(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);

@@ -27,7 +27,7 @@ _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMED
 # Every symbol include/rhyme_gpu.h declares.
 EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rhyme_gpu_last_error",
            "rhyme_gpu_get_stream", "rhyme_gpu_register_box", "rhyme_gpu_unregister_box",
-           "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step",
+           "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step", "rhyme_gpu_cfl_dt",
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
@@ -99,6 +99,8 @@ def load():
     L.rhyme_gpu_sync_to_host.argtypes = [vp, C.c_int]
     L.rhyme_gpu_cfl_time_step.argtypes = [vp, C.c_int, dp, dp]
     L.rhyme_gpu_set_boundaries.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_cfl_dt.argtypes = [vp, C.c_int, dp]
+    L.rhyme_gpu_cfl_dt.restype = C.c_double
     L.rhyme_gpu_mh_solve.argtypes = [vp, C.c_int, dp, C.c_double]
     L.rhyme_gpu_run.argtypes = [vp, C.c_int, dp, C.c_int, dp]
     L.rhyme_gpu_synchronize.argtypes = [vp]
