@@ -192,6 +192,41 @@ int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  */
 int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count);
 
+/*
+ * No counterpart in the reference: one plain-FP64 MUSCL-Hancock update
+ * (the same kernels as rhyme_gpu_mh_solve) that allocates nothing, for
+ * callers that cannot allocate device memory: hosts whose device arrays come
+ * from their own pool or from a Fortran runtime (CUDA Fortran, OpenACC) and
+ * that keep all device allocations under their own control, or runs under a
+ * fixed device-memory budget where an allocation in the middle of a step
+ * could fail or synchronize the device.
+ *
+ *  - d_cells_in / d_cells_out: device pointers to the NDIM+2 hydro component
+ *    blocks of the box in the layout of rhyme_gpu_register_box, ghosts of
+ *    d_cells_in already filled. The interior of d_cells_out receives U^{n+1};
+ *    its ghosts are not written. d_cells_out may equal d_cells_in.
+ *  - params->precision must be RHYME_GPU_FP64.
+ *  - Scratch: a fixed device array of RHYME_GPU_NOALLOC_SCRATCH_DOUBLES
+ *    doubles (16 MiB) inside this library, which every GPU that loads the
+ *    library holds until the process exits. A box needs
+ *    32 + 3*NDIM*(NDIM+2)*prod(N_a + 4) doubles (a 2-D 291^2 box, a 3-D
+ *    32^3 box); larger boxes are rejected with RHYME_GPU_EINVAL and a
+ *    message on stderr.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls on a device share the array: calls whose work overlaps on the
+ *    GPU (different streams, no ordering between them) race. Nothing in the
+ *    array needs clearing between calls.
+ *  - stream: the cudaStream_t to launch on (NULL: the default stream).
+ *    Asynchronous; errors of the launch are returned, not of the kernels.
+ */
+#define RHYME_GPU_NOALLOC_SCRATCH_DOUBLES (2LL * 1024 * 1024)
+int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params,
+                               const double* d_cells_in, double* d_cells_out,
+                               const int dims[3], const double dx[3], double dt,
+                               void* stream);
+
 /* Waits (bounded) for all work on the context stream. */
 int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);
 

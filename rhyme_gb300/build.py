@@ -26,6 +26,7 @@ UNITS = {
     "kernels_elem.cu": ["--fmad=false"],
     "rhyme_gpu.cu": ["--fmad=false"],
     "kernels_mixed.cu": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h"]
 

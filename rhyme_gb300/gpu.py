@@ -31,7 +31,7 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
-           "rhyme_gpu_fallback_count"]
+           "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc"]
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 
 
@@ -111,6 +111,7 @@ def load():
     L.rhyme_gpu_profile_steps.argtypes = [vp, C.c_int, dp, C.c_int, dp]
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
+    L.rhyme_gpu_mh_solve_noalloc.argtypes = [C.POINTER(Params), vp, vp, ip, dp, C.c_double, vp]
     _lib = L
     return L
 
