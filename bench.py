@@ -38,8 +38,18 @@ METRIC = "cell-updates/s"
 L2_FLUSH_BYTES = 512 << 20
 
 
-def workload(name):
+def workload(name, precision="fp64"):
     """(cells, dx, params, config dict) of a named workload."""
+    from rhyme_gb300 import ic
+    cells, dx, p, cfg = _workload(name)
+    if precision == "mixed":
+        from rhyme_gb300.params import MIXED
+        p = dict(p, precision=MIXED)
+        cfg = dict(cfg, workload=cfg["workload"].replace("plain FP64", "mixed FP32/FP64"))
+    return cells, dx, p, cfg
+
+
+def _workload(name):
     from rhyme_gb300 import ic
     if name == "slab2d":
         cells, dx, p = ic.slab_2d(n=256, seed=0)
@@ -197,6 +207,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     cells, dx, p, cfg = workload(args.workload)
+    p = dict(p, precision=0)  # the CPU implementation is FP64
     import oracle
     nthreads = os.cpu_count() or 1
     interior = cfg["cells"]
@@ -223,7 +234,7 @@ def run_gpu(args, rank, local, world):
     import torch
     from rhyme_gb300 import gpu
     torch.cuda.set_device(local)
-    cells, dx, p, cfg = workload(args.workload)
+    cells, dx, p, cfg = workload(args.workload, args.precision)
     ndim = p["ndim"]
     interior = cfg["cells"]
     K, W = args.steps, args.warmup
@@ -303,7 +314,8 @@ def run_gpu(args, rank, local, world):
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "ms_per_step_median": statistics.median(per_step),
                 "ms_per_step_max": max(per_step), "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "data": "synthetic",
                 "config": dict(cfg, l2="flushed (512 MiB write) between timed steps, outside the events",
                                parallelism="replicas" if world > 1 else "single box"),
                 "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": hydro_bytes + 8,
@@ -312,7 +324,8 @@ def run_gpu(args, rank, local, world):
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": traffic, "bytes_per_cell_update": bpc,
                              "note": "the plain FP64 path is bound by the FP64 pipe, not HBM"},
-                "phases_ms": phases, "clocks": clk, "gpu_launches": 5 * K,
+                "phases_ms": phases, "clocks": clk,
+                "gpu_launches": (5 if args.precision == "fp64" else 3 + ndim) * K,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     ctx2.close()
@@ -329,6 +342,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("at least 3 warm-up steps")
