@@ -12,8 +12,13 @@
 // conserved component and cell, since on GB300 even FP64 adds are scarce.
 //
 // Interfaces that near vacuum, or whose FP32 Newton iteration misses the
-// tolerance on its first guess, are queued per CTA in shared memory and
-// redone with the FP64 Riemann solver (same device code, double).
+// tolerance on its first guess, get a zero flux in the sweep and are appended
+// (once, by the tile that owns them) to a device queue with their FP32 face
+// states. After the last sweep one kernel solves the queued interfaces with
+// the FP64 Riemann solver (same device code, double) and applies
+// -+ dt/dx * F to the two adjacent interior cells of U^{n+1}; a second one
+// refreshes their FP32 mirror. Keeping the FP64 code out of the sweeps keeps
+// them at ~64 registers (it tripled their register count inline).
 //
 // The CFL maximum of the mixed path is taken in FP32 over Uf; dt itself is
 // formed in FP64.
@@ -134,15 +139,13 @@ struct SweepSmem {
   float ul[D + 2][(S + 2) * P];  // face states, left / right
   float ur[D + 2][(S + 2) * P];
   float f[D + 2][(S + 1) * P];   // interface fluxes
-  int nfb;                       // FP64 fallback queue
-  short fb[(S + 1) * P];
 };
 
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
-                 double* __restrict__ Unew, float* __restrict__ Ufnew, int* __restrict__ fb_count) {
+                 double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   __shared__ SweepSmem<D, S, P> sh;
   const int NA = g.n[A];
@@ -154,9 +157,13 @@ __global__ void __launch_bounds__(kThreads)
   const int b0 = tB * P + 1;
   const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
   const long long F = g.field;
-  const double dt = *dtp;
-  const float dtdx = (float)(dt / dx.v[A]);
-  const float hdtdx = (float)(0.5 * dt / dx.v[A]);
+  // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on GB300)
+  __shared__ float s_dtdx[2];
+  if (threadIdx.x == 0) {
+    const double dt = *dtp;
+    s_dtdx[0] = (float)(dt / dx.v[A]);
+    s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+  }
 
   auto offset = [&](int ga, int gb) -> long long {
     int c3[3] = {1, 1, 1};
@@ -177,7 +184,6 @@ __global__ void __launch_bounds__(kThreads)
   };
   auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
 
-  if (threadIdx.x == 0) sh.nfb = 0;
   // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
   for (int it = threadIdx.x; it < (S + 4) * P; it += kThreads) {
     int la, lb;
@@ -189,6 +195,8 @@ __global__ void __launch_bounds__(kThreads)
     for (int c = 0; c < D + 2; ++c) sh.u[c][ix(la, lb, S + 4)] = ok ? Uf[(long long)c * F + o] : 0.f;
   }
   __syncthreads();
+  const float dtdx = s_dtdx[0];
+  const float hdtdx = s_dtdx[1];
 
   // 2. face states of cells a0-1 .. min(a0+S, NA+1)
   for (int it = threadIdx.x; it < (S + 2) * P; it += kThreads) {
@@ -231,31 +239,32 @@ __global__ void __launch_bounds__(kThreads)
         if (!isfinite(f[c])) need64 = true;
     }
     if (need64) {
-      const int q = atomicAdd(&sh.nfb, 1);
-      sh.fb[q] = (short)it;
-    } else {
+      // zero here; the FP64 correction is applied after the last sweep.
+      // Each interface is queued once: by the tile whose left face it is,
+      // or by the last tile for the box's right boundary.
+      const int ga = a0 - 1 + li;
+      if (li < S || ga == NA) {
+        const int slot = atomicAdd(q.n, 1);
+        if (slot < q.cap) {
+          FallbackEntry& e = q.e[slot];
+          e.axis = A;
+          e.ga = ga;
+          e.o = offset(ga, b0 + lb);
 #pragma unroll
-      for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = f[c];
+          for (int c = 0; c < D + 2; ++c) {
+            e.l[c] = l[c];
+            e.r[c] = r[c];
+          }
+        } else {
+          atomicOr(q.status, 2);  // queue full: the interface keeps a zero flux
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c) f[c] = 0.f;
     }
-  }
-  __syncthreads();
-
-  // 3b. queued interfaces in FP64, one per thread
-  const int nfb = sh.nfb;
-  for (int q = threadIdx.x; q < nfb; q += kThreads) {
-    int li, lb;
-    split(sh.fb[q], S + 1, li, lb);
-    double l[D + 2], r[D + 2], f[D + 2];
 #pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      l[c] = (double)sh.ur[c][ix(li, lb, S + 2)];
-      r[c] = (double)sh.ul[c][ix(li + 1, lb, S + 2)];
-    }
-    interface_flux<D, A>(M.G64, M.rp64, l, r, f);
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = (float)f[c];
+    for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = f[c];
   }
-  if (fb_count && threadIdx.x == 0 && nfb > 0) atomicAdd(fb_count, nfb);
   __syncthreads();
 
   // 4. flux differences of cells a0 .. a0+S-1 and the accumulation
@@ -286,7 +295,7 @@ __global__ void __launch_bounds__(kThreads)
 template <int D, int A, int S, int P, int MODE>
 cudaError_t launch_sweep(const MixedParams& M, const float* Uf, const double* U, const Geom& g,
                          const Dx& dx, const double* dtp, float* acc, double* Unew, float* Ufnew,
-                         int* fb_count, cudaStream_t st) {
+                         const FallbackQueue& q, cudaStream_t st) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   const int NA = g.n[A];
   const int NB = (B < D) ? g.n[B] : 1;
@@ -297,8 +306,73 @@ cudaError_t launch_sweep(const MixedParams& M, const float* Uf, const double* U,
   } else {
     grid = dim3((NB + P - 1) / P, (NA + S - 1) / S, NC);
   }
-  sweep_kernel<D, A, S, P, MODE><<<grid, kThreads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew,
-                                                            fb_count);
+  sweep_kernel<D, A, S, P, MODE><<<grid, kThreads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q);
+  return cudaGetLastError();
+}
+
+// FP64 Riemann problems of the queued interfaces; -+ dt/dx * F applied to
+// the adjacent interior cells of U^{n+1} (atomically: a cell can border two
+// queued interfaces).
+template <int D>
+__global__ void __launch_bounds__(128)
+    fallback_fix_kernel(MixedParams M, FallbackQueue q, Geom g, Dx dx, const double* __restrict__ dtp,
+                        double* __restrict__ Unew) {
+  const int n = min(*q.n, q.cap);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(q.total, n);
+  const double dt = *dtp;
+  const long long F = g.field;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const FallbackEntry e = q.e[i];
+    double l[D + 2], r[D + 2], f[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      l[c] = (double)e.l[c];
+      r[c] = (double)e.r[c];
+    }
+    if (e.axis == 0) interface_flux<D, 0>(M.G64, M.rp64, l, r, f);
+    if constexpr (D > 1) {
+      if (e.axis == 1) interface_flux<D, 1>(M.G64, M.rp64, l, r, f);
+    }
+    if constexpr (D > 2) {
+      if (e.axis == 2) interface_flux<D, 2>(M.G64, M.rp64, l, r, f);
+    }
+    const double dtdx = dt / dx.v[e.axis];
+    const long long sa = g.s[e.axis];
+    const int NA = g.n[e.axis];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const double corr = dtdx * f[c];
+      if (e.ga >= 1) atomicAdd(&Unew[(long long)c * F + e.o], -corr);
+      if (e.ga + 1 <= NA) atomicAdd(&Unew[(long long)c * F + e.o + sa], corr);
+    }
+  }
+}
+
+// FP32 mirror of the cells the fix-up touched.
+template <int D>
+__global__ void __launch_bounds__(256)
+    fallback_refresh_kernel(FallbackQueue q, Geom g, const double* __restrict__ Unew,
+                            float* __restrict__ Ufnew) {
+  const int n = min(*q.n, q.cap);
+  const long long F = g.field;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const FallbackEntry e = q.e[i];
+    const long long sa = g.s[e.axis];
+    const int NA = g.n[e.axis];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const long long oc = (long long)c * F + e.o;
+      if (e.ga >= 1) Ufnew[oc] = (float)Unew[oc];
+      if (e.ga + 1 <= NA) Ufnew[oc + sa] = (float)Unew[oc + sa];
+    }
+  }
+}
+
+template <int D>
+cudaError_t launch_fallback(const MixedParams& M, const FallbackQueue& q, const Geom& g, const Dx& dx,
+                            const double* dtp, double* Unew, float* Ufnew, cudaStream_t st) {
+  fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, g, dx, dtp, Unew);
+  fallback_refresh_kernel<D><<<152, 256, 0, st>>>(q, g, Unew, Ufnew);
   return cudaGetLastError();
 }
 
@@ -325,24 +399,28 @@ cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& 
 
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
                                   double* Unew, float* Ufnew, float* acc, const Geom& g,
-                                  const Dx& dx, const StepScratch& s, int* fb_count,
+                                  const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   cudaStream_t st) {
-  cudaError_t e = cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(q.n, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
   switch (M.ndim) {
     case 1:
-      e = launch_sweep<1, 0, 256, 1, ONLY>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      e = launch_sweep<1, 0, 256, 1, ONLY>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
+      if (e == cudaSuccess) e = launch_fallback<1>(M, q, g, dx, s.dt, Unew, Ufnew, st);
       break;
     case 2:
-      e = launch_sweep<2, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      e = launch_sweep<2, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
       if (e == cudaSuccess)
-        e = launch_sweep<2, 1, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+        e = launch_sweep<2, 1, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
+      if (e == cudaSuccess) e = launch_fallback<2>(M, q, g, dx, s.dt, Unew, Ufnew, st);
       break;
     case 3:
-      e = launch_sweep<3, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+      e = launch_sweep<3, 0, 32, 8, FIRST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
       if (e == cudaSuccess)
-        e = launch_sweep<3, 1, 16, 16, MID>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+        e = launch_sweep<3, 1, 16, 16, MID>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
       if (e == cudaSuccess)
-        e = launch_sweep<3, 2, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, fb_count, st);
+        e = launch_sweep<3, 2, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
+      if (e == cudaSuccess) e = launch_fallback<3>(M, q, g, dx, s.dt, Unew, Ufnew, st);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -33,6 +33,25 @@ struct MixedParams {
   float omega;
 };
 
+// One interface queued for the FP64 Riemann solver by a mixed sweep: its
+// axis, the index along that axis of its left cell (0..N), the offset of the
+// left cell and the FP32 face states on either side.
+struct FallbackEntry {
+  int axis;
+  int ga;
+  long long o;
+  float l[5];
+  float r[5];
+};
+
+struct FallbackQueue {
+  FallbackEntry* e;
+  int* n;       // entries this step (reset before each step)
+  int cap;
+  int* status;  // bit 1: queue overflow
+  int* total;   // running count of FP64 interfaces (statistics)
+};
+
 // Geometry of one box in the reference layout: component blocks of
 // `field` doubles, cell (i,j,k) (1-based interior, ghosts -1..N+2) at
 // (i+1)*s0 + (j+1)*s1 + (k+1)*s2 for the active axes.
@@ -98,7 +117,7 @@ cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& 
                              const Dx& dx, const StepScratch& s, cudaStream_t st);
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
                                   double* Unew, float* Ufnew, float* acc, const Geom& g,
-                                  const Dx& dx, const StepScratch& s, int* fb_count,
+                                  const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   cudaStream_t st);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 

@@ -5,6 +5,7 @@
 // buffers (ping-pong: the unsplit update reads U^n and writes U^{n+1}), the
 // solver scratch, and up to two captured CUDA graphs of one driver step (one
 // per buffer parity) that rhyme_gpu_run replays.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -35,6 +36,7 @@ struct Box {
   float* Uf[2] = {nullptr, nullptr};  // FP32 mirrors of the state (mixed mode)
   float* acc = nullptr;               // FP32 flux-difference accumulator (mixed mode)
   int* fb_count = nullptr;            // interfaces redone in FP64 (mixed mode)
+  FallbackQueue fbq{};                // FP64 fallback queue (mixed mode)
   double* trace_buf = nullptr;
   int* trace_pos = nullptr;
   bool registered_host = false;
@@ -206,6 +208,7 @@ void destroy_box(Box* b) {
     cudaFree(b->Uf[i]);
   }
   cudaFree(b->acc);
+  cudaFree(b->fbq.e);
   cudaFree(b->s.faces);
   cudaFree(b->s.fluxes);
   cudaFree(b->s.dt);
@@ -306,6 +309,9 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   if (ctx->mixed) {
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->Uf[i], (size_t)(D + 2) * F * sizeof(float));
     if (e == cudaSuccess && D > 1) e = cudaMalloc(&b->acc, (size_t)(D + 2) * F * sizeof(float));
+    long long cells = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+    b->fbq.cap = (int)std::min<long long>(std::max<long long>(4096, D * cells / 16), 1LL << 30);
+    if (e == cudaSuccess) e = cudaMalloc(&b->fbq.e, (size_t)b->fbq.cap * sizeof(FallbackEntry));
   } else {
     if (e == cudaSuccess) e = cudaMalloc(&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double));
@@ -325,6 +331,9 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   b->s.status = (int*)(base + 20);
   b->trace_pos = (int*)(base + 24);
   b->fb_count = (int*)(base + 28);
+  b->fbq.n = (int*)(base + 32);
+  b->fbq.status = b->s.status;
+  b->fbq.total = b->fb_count;
   b->trace_buf = (double*)(base + 64);
   // Pin the caller's array for asynchronous copies when possible; a failure
   // here only costs copy speed.
@@ -415,7 +424,7 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
     if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
     if (e == cudaSuccess) e = launch_ghost_fill_f32(ctx->dp, b->Uf[cur], b->g, ctx->stream);
     if (e == cudaSuccess)
-      e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fb_count,
+      e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fbq,
                                 ctx->stream);
     return e;
   }
@@ -501,7 +510,7 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->mixed)
     CK(launch_mh_solve_mixed(ctx->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
-                             b->acc, b->g, d, scratch_of(b, false), b->fb_count, ctx->stream));
+                             b->acc, b->g, d, scratch_of(b, false), b->fbq, ctx->stream));
   else
     CK(launch_mh_solve(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
                        ctx->stream));
@@ -674,7 +683,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
       if (e == cudaSuccess) e = cudaEventRecord(ev[3], ctx->stream);
       if (e == cudaSuccess)
         e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
-                                  b->fb_count, ctx->stream);
+                                  b->fbq, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[4], ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[5], ctx->stream);
     } else {

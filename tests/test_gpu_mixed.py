@@ -1,0 +1,112 @@
+"""Mixed-precision path (FP32 reconstruction / Riemann / flux, FP64 state
+accumulation, FP64 Riemann fallback) against the plain FP64 GPU path.
+
+Tolerance: relative L1 of the density <= 1e-6 after the stated steps (the
+bar the mixed form is quoted at); other fields <= 1e-5; dt within 1e-6.
+These workloads do not amplify rounding differences (the 2-D shear slab
+does, and is quoted in FP64 only).
+"""
+import numpy as np
+import pytest
+
+from parity import field_errors
+
+from rhyme_gb300 import gpu, ic
+from rhyme_gb300.params import FP64, MIXED, PERIODIC, REFLECTIVE, VAN_LEER, hydro_params
+
+pytestmark = pytest.mark.gpu
+
+MIXED_L1_RHO = 1e-6
+MIXED_L1_OTHER = 1e-5
+
+
+def run(p, cells, dx, nsteps, precision):
+    c = cells.copy()
+    with gpu.Context(dict(p, precision=precision)) as ctx:
+        box = ctx.register_box(c)
+        dts = ctx.run(box, dx, nsteps)
+        fb = ctx.fallback_count(box)
+        ctx.sync_to_host(box)
+    return c, dts, fb
+
+
+def check(p, cells, dx, nsteps, rho_tol=MIXED_L1_RHO, other_tol=MIXED_L1_OTHER):
+    a, da, _ = run(p, cells, dx, nsteps, FP64)
+    b, db, fb = run(p, cells, dx, nsteps, MIXED)
+    assert np.isfinite(b).all()
+    errs = field_errors(b, a, p["ndim"])
+    assert errs[0][0] <= rho_tol, errs
+    for l1, _ in errs[1:]:
+        assert l1 <= other_tol, errs
+    assert np.max(np.abs(db - da) / da) <= 1e-6
+    return errs, fb
+
+
+def test_mixed_riemann_1d():
+    for seed in (0, 1):
+        cells, dx, p = ic.riemann_1d(n=512, seed=seed)
+        errs, _ = check(p, cells, dx, 100)
+        print("1-D riemann seed", seed, errs)
+
+
+def test_mixed_acoustic_pulse_2d():
+    """A smooth 2-D pressure pulse (no shear layer), periodic, van Leer."""
+    n = 96
+    g = 5.0 / 3.0
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    r2 = (X - 0.5) ** 2 + (Y - 0.5) ** 2
+    rho = 1.0 + 0.2 * np.exp(-r2 / 0.01)
+    pr = 1.0 + 0.5 * np.exp(-r2 / 0.01)
+    cells = ic.empty_box(2, [n, n])
+    cells[:, 2:-2, 2:-2] = ic.prim_to_cons(rho, [np.zeros_like(rho)] * 2, pr, g)
+    p = hydro_params(2, limiter=VAN_LEER, bc=[PERIODIC] * 4, courant=0.5)
+    errs, _ = check(p, cells, [1.0 / n] * 2, 150)
+    print("2-D pulse", errs)
+
+
+def test_mixed_spheres_3d():
+    cells, dx, p = ic.spheres_3d(n=64, nspheres=32, seed=0)
+    errs, _ = check(p, cells, dx, 100)
+    print("3-D spheres 64^3", errs)
+
+
+def test_mixed_fallback_near_vacuum():
+    """Two strongly receding states open a near-vacuum gap: those interfaces
+    go to the FP64 solver and the result stays finite and close to FP64."""
+    n = 256
+    g = 5.0 / 3.0
+    cells = ic.empty_box(1, [n])
+    x = np.arange(n)
+    rho = np.ones(n)
+    u = np.where(x < n // 2, -3.0, 3.0)
+    pr = np.full(n, 0.05)
+    cells[:, 2:-2] = ic.prim_to_cons(rho, [u], pr, g)
+    p = hydro_params(1, limiter=VAN_LEER, bc=[REFLECTIVE] * 2, vac_rho=1e-8, vac_p=1e-10, courant=0.5)
+    a, da, _ = run(p, cells, [1.0 / n], 40, FP64)
+    b, db, fb = run(p, cells, [1.0 / n], 40, MIXED)
+    assert fb > 0
+    assert np.isfinite(b).all()
+    errs = field_errors(b, a, 1)
+    assert errs[0][0] <= 1e-4, errs
+    print("near-vacuum 1-D: FP64 interfaces", fb, "errors", errs)
+
+
+def test_mixed_stepwise_api_matches_run():
+    cells, dx, p = ic.spheres_3d(n=32, nspheres=4, seed=2)
+    q = dict(p, precision=MIXED)
+    a = cells.copy()
+    b = cells.copy()
+    with gpu.Context(q) as ctx:
+        box = ctx.register_box(a)
+        ctx.run(box, dx, 5)
+        ctx.sync_to_host(box)
+    with gpu.Context(q) as ctx:
+        box = ctx.register_box(b)
+        for _ in range(5):
+            dt = ctx.cfl_time_step(box, dx)
+            ctx.set_boundaries(box)
+            ctx.muscl_hancock_solve(box, dx, dt)
+        ctx.sync_to_host(box)
+    errs = field_errors(b, a, 3)
+    assert max(e[0] for e in errs) <= 1e-12, errs
