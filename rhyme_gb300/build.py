@@ -27,8 +27,9 @@ UNITS = {
     "rhyme_gpu.cu": ["--fmad=false"],
     "kernels_mixed.cu": [],
     "noalloc.cu": ["--fmad=false"],
+    "kernels_batch.cu": ["--fmad=false"],
 }
-HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h"]
+HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "box_elems.cuh"]
 
 
 def nvcc():

@@ -17,7 +17,7 @@
 // the same IEEE operations, in the same order, as the reference.
 #include <cstdio>
 
-#include "rgpu_internal.h"
+#include "box_elems.cuh"
 
 namespace rgpu {
 
@@ -45,70 +45,11 @@ inline int grid_for(long long total, int block) {
 // holds after the fill.
 template <int D, typename T>
 __global__ void __launch_bounds__(kFillBlock)
-    ghost_fill_kernel(DevParams P, T* __restrict__ U, T* __restrict__ M, Geom g,
-                      long long off1, long long off2, long long total) {
+    ghost_fill_kernel(BoxRules R, T* __restrict__ U, T* __restrict__ M, Geom g, long long off1,
+                      long long off2, long long total) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    int axis;
-    long long r;
-    if (t < off1) {
-      axis = 0;
-      r = t;
-    } else if (t < off2) {
-      axis = 1;
-      r = t - off1;
-    } else {
-      axis = 2;
-      r = t - off2;
-    }
-    const int t1 = (axis == 0) ? 1 : 0, t2 = (axis == 2) ? 1 : 2;
-    const int n1 = (t1 < D) ? g.n[t1] : 1, n2 = (t2 < D) ? g.n[t2] : 1;
-    const long long per_c = (long long)n1 * n2;
-    const int c = (int)(r / per_c);
-    const long long q = r - (long long)c * per_c;
-    int idx[3] = {1, 1, 1};
-    idx[t1] = (int)(q % n1) + 1;
-    idx[t2] = (int)(q / n1) + 1;
-    idx[axis] = 0;
-    const long long base = g.at(D, idx[0], idx[1], idx[2]);  // cell 0 of the line
-    const long long sa = g.s[axis];
-    const long long N = g.n[axis];
-    T* f = U + (long long)c * g.field;
-    for (int side = 0; side < 2; ++side) {
-      const int type = P.bc[2 * axis + side];
-      long long g0, g1, s0, s1;
-      if (side == 0) {
-        g0 = base;
-        g1 = base - sa;
-        s0 = (type == 3) ? base + N * sa : base + sa;
-        s1 = (type == 3) ? base + (N - 1) * sa : base + 2 * sa;
-      } else {
-        g0 = base + (N + 1) * sa;
-        g1 = base + (N + 2) * sa;
-        s0 = (type == 3) ? base + sa : base + N * sa;
-        s1 = (type == 3) ? base + 2 * sa : base + (N - 1) * sa;
-      }
-      if (type == 4) {  // inflow
-        const T v = (T)P.inflow[2 * axis + side][c];
-        f[g0] = v;
-        f[g1] = v;
-      } else if (type >= 1 && type <= 3) {
-        f[g0] = f[s0];
-        f[g1] = f[s1];
-        if (type == 1 && c == 1 + axis) {  // reflective: negate normal momentum
-          f[g0] = -f[s0];
-          f[g1] = -f[s1];
-        }
-      } else {
-        continue;
-      }
-      if (M) {
-        T* m = M + (long long)c * g.field;
-        m[g0] = f[g0];
-        m[g1] = f[g1];
-      }
-    }
-  }
+       t += (long long)gridDim.x * blockDim.x)
+    ghost_elem<D, T>(R, U, M, g, off1, off2, t);
 }
 
 // ------------------------------------------------------------------ K2 ---
@@ -120,26 +61,13 @@ __global__ void __launch_bounds__(kFillBlock)
 template <int D>
 __global__ void __launch_bounds__(kCflBlock)
     cfl_kernel(DevParams P, const double* __restrict__ U, Geom g, double mdx, StepScratch s) {
-  const long long n0 = g.n[0], n1 = g.n[1];
-  const long long total = n0 * n1 * (long long)g.n[2];
+  const long long total = (long long)g.n[0] * g.n[1] * (long long)g.n[2];
   double m = 0.0;
   int bad = 0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % n0) + 1;
-    const long long q = t / n0;
-    const int j = (int)(q % n1) + 1;
-    const int k = (int)(q / n1) + 1;
-    const long long o = g.at(D, i, j, k);
-    double u[D + 2];
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) u[c] = U[(long long)c * g.field + o];
-    double ss = 0.0;
-#pragma unroll
-    for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
-    const double v = sqrt(ss) / u[0] + sound_speed<D>(P.G, u);
+    const double v = signal_speed_elem<D>(P.G, U, g, t, bad);
     if (v > m) m = v;
-    if (!(u[0] > 0.0) || !isfinite(v)) bad = 1;
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -187,115 +115,53 @@ __global__ void __launch_bounds__(kCflBlock)
 }
 
 // ------------------------------------------------------------------ K3 ---
-// Pass 1 (loop 1 of the memory-intensive solver): limited slopes and
-// half-step face states ul, ur of every cell with i_AX in [0, N+1] and
-// interior transverse coordinates, along axis AX.
-template <int D, int AX>
-__device__ __forceinline__ void faces_body(const DevParams& P, const double* __restrict__ U,
-                                           const Geom& g, double hdtdx, double* __restrict__ FS) {
-  int e[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) e[a] = (a == AX) ? g.n[a] + 2 : g.n[a];
-  const long long total = (long long)e[0] * e[1] * e[2];
-  const long long F = g.field;
-  const long long sa = g.s[AX];
-  double* ul = FS + (long long)(AX * 2 + 0) * (D + 2) * F;
-  double* ur = FS + (long long)(AX * 2 + 1) * (D + 2) * F;
-  const double w = P.omega;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    int c3[3];
-    c3[0] = (int)(t % e[0]);
-    const long long q = t / e[0];
-    c3[1] = (int)(q % e[1]);
-    c3[2] = (int)(q / e[1]);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) c3[a] += (a == AX) ? 0 : 1;
-    const long long o = g.at(D, c3[0], c3[1], c3[2]);
-    double um[D + 2], u0[D + 2], up[D + 2], l[D + 2], r[D + 2];
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      const double* f = U + (long long)c * F + o;
-      um[c] = f[-sa];
-      u0[c] = f[0];
-      up[c] = f[sa];
-    }
-    face_states<D, AX>(P.G, P.limiter, w, um, u0, up, hdtdx, l, r);
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      ul[(long long)c * F + o] = l[c];
-      ur[(long long)c * F + o] = r[c];
-    }
-  }
-}
-
+// Pass 1: face states of every cell with i_AX in [0, N+1] (box_elems.cuh).
 template <int D>
 __global__ void __launch_bounds__(kFaceBlock)
-    faces_kernel(DevParams P, const double* __restrict__ U, Geom g, Dx dx, const double* dtp,
-                 double* __restrict__ FS) {
+    faces_kernel(DevParams P, BoxRules R, const double* __restrict__ U, Geom g, Dx dx,
+                 const double* dtp, double* __restrict__ FS) {
   const double dt = *dtp;
   const int axis = blockIdx.y;
-  if (axis == 0) faces_body<D, 0>(P, U, g, 0.5 * dt / dx.v[0], FS);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (axis == 0) {
+    const double h = 0.5 * dt / dx.v[0];
+    for (long long t = t0; t < face_count<0>(g); t += stride) faces_elem<D, 0>(P.G, R, U, g, h, FS, t);
+  }
   if constexpr (D > 1) {
-    if (axis == 1) faces_body<D, 1>(P, U, g, 0.5 * dt / dx.v[1], FS);
+    if (axis == 1) {
+      const double h = 0.5 * dt / dx.v[1];
+      for (long long t = t0; t < face_count<1>(g); t += stride) faces_elem<D, 1>(P.G, R, U, g, h, FS, t);
+    }
   }
   if constexpr (D > 2) {
-    if (axis == 2) faces_body<D, 2>(P, U, g, 0.5 * dt / dx.v[2], FS);
-  }
-}
-
-// Pass 2 (loop 2): exact Riemann problem between ur of cell i and ul of
-// cell i+1 along AX, sampled at x/t = 0, and its flux, for i_AX in [0, N].
-template <int D, int AX>
-__device__ __forceinline__ void flux_body(const DevParams& P, const double* __restrict__ FS,
-                                          const Geom& g, double* __restrict__ FR) {
-  int e[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) e[a] = (a == AX) ? g.n[a] + 1 : g.n[a];
-  const long long total = (long long)e[0] * e[1] * e[2];
-  const long long F = g.field;
-  const long long sa = g.s[AX];
-  const double* ul = FS + (long long)(AX * 2 + 0) * (D + 2) * F;
-  const double* ur = FS + (long long)(AX * 2 + 1) * (D + 2) * F;
-  double* fr = FR + (long long)AX * (D + 2) * F;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    int c3[3];
-    c3[0] = (int)(t % e[0]);
-    const long long q = t / e[0];
-    c3[1] = (int)(q % e[1]);
-    c3[2] = (int)(q / e[1]);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) c3[a] += (a == AX) ? 0 : 1;
-    const long long o = g.at(D, c3[0], c3[1], c3[2]);
-    double l[D + 2], r[D + 2], f[D + 2];
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      l[c] = ur[(long long)c * F + o];
-      r[c] = ul[(long long)c * F + o + sa];
+    if (axis == 2) {
+      const double h = 0.5 * dt / dx.v[2];
+      for (long long t = t0; t < face_count<2>(g); t += stride) faces_elem<D, 2>(P.G, R, U, g, h, FS, t);
     }
-    interface_flux<D, AX>(P.G, P.rp, l, r, f);
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) fr[(long long)c * F + o] = f[c];
   }
 }
 
+// Pass 2: exact Riemann problem and flux of every interface, i_AX in [0, N].
 template <int D>
 __global__ void __launch_bounds__(kFluxBlock)
     flux_kernel(DevParams P, const double* __restrict__ FS, Geom g, double* __restrict__ FR) {
   const int axis = blockIdx.y;
-  if (axis == 0) flux_body<D, 0>(P, FS, g, FR);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (axis == 0)
+    for (long long t = t0; t < iface_count<0>(g); t += stride) flux_elem<D, 0>(P.G, P.rp, FS, g, FR, t);
   if constexpr (D > 1) {
-    if (axis == 1) flux_body<D, 1>(P, FS, g, FR);
+    if (axis == 1)
+      for (long long t = t0; t < iface_count<1>(g); t += stride) flux_elem<D, 1>(P.G, P.rp, FS, g, FR, t);
   }
   if constexpr (D > 2) {
-    if (axis == 2) flux_body<D, 2>(P, FS, g, FR);
+    if (axis == 2)
+      for (long long t = t0; t < iface_count<2>(g); t += stride) flux_elem<D, 2>(P.G, P.rp, FS, g, FR, t);
   }
 }
 
-// Pass 3 (loop 3): U^{n+1} = U + ((X + Y) + Z) with X = dt/dx*(F(i-1)-F(i)),
-// written to the other state buffer; or, for the cpu-intensive solver,
-// ((U + X) + Y) + Z (rhyme_muscl_hancock_solve_cpu_intensive.f90:117-136).
+// Pass 3: U^{n+1} of every interior cell, written to the other buffer.
 template <int D>
 __global__ void __launch_bounds__(kUpdBlock)
     update_kernel(DevParams P, const double* __restrict__ U, const double* __restrict__ FR,
@@ -304,40 +170,10 @@ __global__ void __launch_bounds__(kUpdBlock)
   double dtdx[3];
 #pragma unroll
   for (int a = 0; a < D; ++a) dtdx[a] = dt / dx.v[a];
-  const long long n0 = g.n[0], n1 = g.n[1];
-  const long long total = n0 * n1 * (long long)g.n[2];
-  const long long F = g.field;
-  const bool cpu_order = (P.solver_type == 1);
+  const long long total = (long long)g.n[0] * g.n[1] * (long long)g.n[2];
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % n0) + 1;
-    const long long q = t / n0;
-    const int j = (int)(q % n1) + 1;
-    const int k = (int)(q / n1) + 1;
-    const long long o = g.at(D, i, j, k);
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      double d[3];
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        const double* fr = FR + ((long long)a * (D + 2) + c) * F + o;
-        d[a] = dtdx[a] * (fr[-g.s[a]] - fr[0]);
-      }
-      const double u = U[(long long)c * F + o];
-      double out;
-      if (cpu_order) {
-        out = u;
-#pragma unroll
-        for (int a = 0; a < D; ++a) out = out + d[a];
-      } else {
-        double acc = d[0];
-#pragma unroll
-        for (int a = 1; a < D; ++a) acc = acc + d[a];
-        out = u + acc;
-      }
-      Unew[(long long)c * F + o] = out;
-    }
-  }
+       t += (long long)gridDim.x * blockDim.x)
+    update_elem<D>(P.solver_type, U, FR, g, dtdx, Unew, t);
 }
 
 template <int D>
@@ -355,7 +191,7 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
   }
   if (ev) cudaEventRecord(ev[0], st);
   dim3 gf(grid_for(tot_f, kFaceBlock), D);
-  faces_kernel<D><<<gf, kFaceBlock, 0, st>>>(P, U, g, dx, s.dt, s.faces);
+  faces_kernel<D><<<gf, kFaceBlock, 0, st>>>(P, rules_of(P), U, g, dx, s.dt, s.faces);
   if (ev) cudaEventRecord(ev[1], st);
   dim3 gr(grid_for(tot_r, kFluxBlock), D);
   flux_kernel<D><<<gr, kFluxBlock, 0, st>>>(P, s.faces, g, s.fluxes);
@@ -371,25 +207,24 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
 
 int max_cfl_blocks() { return kMaxBlocks; }
 
+template <int D, typename T>
+cudaError_t ghost_fill_d(const BoxRules& R, T* U, T* U_mirror, const Geom& g, cudaStream_t st) {
+  long long off1, off2, total;
+  ghost_offsets<D>(g, off1, off2, total);
+  ghost_fill_kernel<D, T><<<grid_for(total, kFillBlock), kFillBlock, 0, st>>>(R, U, U_mirror, g, off1, off2,
+                                                                              total);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t ghost_fill_any(const DevParams& P, T* U, T* U_mirror, const Geom& g, cudaStream_t st) {
-  const int D = P.ndim;
-  long long per_axis[3] = {0, 0, 0};
-  for (int a = 0; a < D; ++a) {
-    long long t = D + 2;
-    for (int b = 0; b < D; ++b)
-      if (b != a) t *= g.n[b];
-    per_axis[a] = t;
+  const BoxRules R = rules_of(P);
+  switch (P.ndim) {
+    case 1: return ghost_fill_d<1, T>(R, U, U_mirror, g, st);
+    case 2: return ghost_fill_d<2, T>(R, U, U_mirror, g, st);
+    case 3: return ghost_fill_d<3, T>(R, U, U_mirror, g, st);
   }
-  const long long off1 = per_axis[0], off2 = off1 + per_axis[1], total = off2 + per_axis[2];
-  const int grid = grid_for(total, kFillBlock);
-  switch (D) {
-    case 1: ghost_fill_kernel<1, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
-    case 2: ghost_fill_kernel<2, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
-    case 3: ghost_fill_kernel<3, T><<<grid, kFillBlock, 0, st>>>(P, U, U_mirror, g, off1, off2, total); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,

@@ -141,24 +141,24 @@ struct SweepSmem {
   float f[D + 2][(S + 1) * P];   // interface fluxes
 };
 
+// One slab (tile tA along the sweep axis, tB across the pencils, plane cC)
+// of a sweep. `box` tags queued FP64 interfaces (0 for a single box).
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(kThreads, 4)
-    sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
-                 Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
-                 double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
+__device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, float omega,
+                                           const float* __restrict__ Uf, const double* __restrict__ U,
+                                           const Geom& g, const Dx& dx, const double* __restrict__ dtp,
+                                           float* __restrict__ acc, double* __restrict__ Unew,
+                                           float* __restrict__ Ufnew, const FallbackQueue& q, int box,
+                                           int tA, int tB, int cC, SweepSmem<D, S, P>& sh) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
-  __shared__ SweepSmem<D, S, P> sh;
   const int NA = g.n[A];
   const int NB = (B < D) ? g.n[B] : 1;
-  // tile origin: the fast grid axis runs along x
-  const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
-  const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
   const int a0 = tA * S + 1;  // first interior cell of the slab along A
   const int b0 = tB * P + 1;
-  const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
   const long long F = g.field;
   // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on GB300)
   __shared__ float s_dtdx[2];
+  __syncthreads();  // the previous tile of this CTA is done with the smem
   if (threadIdx.x == 0) {
     const double dt = *dtp;
     s_dtdx[0] = (float)(dt / dx.v[A]);
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(kThreads, 4)
       u0[c] = sh.u[c][ix(la + 1, lb, S + 4)];
       up[c] = sh.u[c][ix(la + 2, lb, S + 4)];
     }
-    face_states<D, A>(M.G, M.limiter, M.omega, um, u0, up, hdtdx, l, r);
+    face_states<D, A>(M.G, limiter, omega, um, u0, up, hdtdx, l, r);
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) {
       sh.ul[c][ix(la, lb, S + 2)] = l[c];
@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(kThreads, 4)
           FallbackEntry& e = q.e[slot];
           e.axis = A;
           e.ga = ga;
+          e.box = box;
           e.o = offset(ga, b0 + lb);
 #pragma unroll
           for (int c = 0; c < D + 2; ++c) {
@@ -289,6 +290,49 @@ __global__ void __launch_bounds__(kThreads, 4)
         Ufnew[oc] = (float)un;
       }
     }
+  }
+}
+
+template <int D, int A, int S, int P, int MODE>
+__global__ void __launch_bounds__(kThreads, 4)
+    sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
+                 Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
+                 double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
+  constexpr int C = Axes<D, A>::C;
+  __shared__ SweepSmem<D, S, P> sh;
+  // tile origin: the fast grid axis runs along x
+  const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
+  const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
+  const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
+  sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, 0, tA, tB, cC,
+                               sh);
+}
+
+// The same sweep over the tiles of a batch of boxes, taken from a work queue
+// (item.chunk = the tile's linear index tA + nA * (tB + nB * (cC - 1))).
+template <int D, int A, int S, int P, int MODE>
+__global__ void __launch_bounds__(kThreads, 4)
+    batch_sweep_kernel(MixedParams M, const BoxDesc* __restrict__ TB, const WorkItem* __restrict__ items,
+                       int n, int* head, FallbackQueue q) {
+  constexpr int B = Axes<D, A>::B;
+  __shared__ SweepSmem<D, S, P> sh;
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n) break;
+    const WorkItem w = items[it];
+    const BoxDesc& b = TB[w.box];
+    const int nA = (b.g.n[A] + S - 1) / S;
+    const int nB = ((B < D ? b.g.n[B] : 1) + P - 1) / P;
+    const int tA = (int)(w.chunk % nA);
+    const long long r = w.chunk / nA;
+    const int tB = (int)(r % nB);
+    const int cC = (int)(r / nB) + 1;
+    sweep_tile<D, A, S, P, MODE>(M, b.limiter, b.omega_f, b.Uf, b.U, b.g, b.dx, b.ctl, b.acc, b.V, b.Vf,
+                                 q, w.box, tA, tB, cC, sh);
   }
 }
 
@@ -376,6 +420,77 @@ cudaError_t launch_fallback(const MixedParams& M, const FallbackQueue& q, const 
   return cudaGetLastError();
 }
 
+// Batched FP64 fix-up: as fallback_fix_kernel, with the box of each entry.
+template <int D>
+__global__ void __launch_bounds__(128)
+    batch_fallback_fix_kernel(MixedParams M, FallbackQueue q, const BoxDesc* __restrict__ TB) {
+  const int n = min(*q.n, q.cap);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(q.total, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const FallbackEntry e = q.e[i];
+    const BoxDesc& b = TB[e.box];
+    double l[D + 2], r[D + 2], f[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      l[c] = (double)e.l[c];
+      r[c] = (double)e.r[c];
+    }
+    if (e.axis == 0) interface_flux<D, 0>(M.G64, M.rp64, l, r, f);
+    if constexpr (D > 1) {
+      if (e.axis == 1) interface_flux<D, 1>(M.G64, M.rp64, l, r, f);
+    }
+    if constexpr (D > 2) {
+      if (e.axis == 2) interface_flux<D, 2>(M.G64, M.rp64, l, r, f);
+    }
+    const double dtdx = b.ctl[0] / b.dx.v[e.axis];
+    const long long sa = b.g.s[e.axis];
+    const int NA = b.g.n[e.axis];
+    const long long F = b.g.field;
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const double corr = dtdx * f[c];
+      if (e.ga >= 1) atomicAdd(&b.V[(long long)c * F + e.o], -corr);
+      if (e.ga + 1 <= NA) atomicAdd(&b.V[(long long)c * F + e.o + sa], corr);
+    }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256)
+    batch_fallback_refresh_kernel(FallbackQueue q, const BoxDesc* __restrict__ TB) {
+  const int n = min(*q.n, q.cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const FallbackEntry e = q.e[i];
+    const BoxDesc& b = TB[e.box];
+    const long long sa = b.g.s[e.axis];
+    const int NA = b.g.n[e.axis];
+    const long long F = b.g.field;
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const long long oc = (long long)c * F + e.o;
+      if (e.ga >= 1) b.Vf[oc] = (float)b.V[oc];
+      if (e.ga + 1 <= NA) b.Vf[oc + sa] = (float)b.V[oc + sa];
+    }
+  }
+}
+
+template <int D, int A, int S, int P, int MODE>
+cudaError_t launch_batch_sweep(const MixedParams& M, const BoxDesc* TB, const BatchLists& L,
+                               const FallbackQueue& q, int slot, cudaStream_t st) {
+  if (L.n_sweep[A] == 0) return cudaSuccess;
+  batch_sweep_kernel<D, A, S, P, MODE><<<152 * 4, kThreads, 0, st>>>(M, TB, L.sweep[A], L.n_sweep[A],
+                                                                     L.heads + slot, q);
+  return cudaGetLastError();
+}
+
+template <int D>
+cudaError_t launch_batch_fallback(const MixedParams& M, const BoxDesc* TB, const FallbackQueue& q,
+                                  cudaStream_t st) {
+  batch_fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, TB);
+  batch_fallback_refresh_kernel<D><<<152, 256, 0, st>>>(q, TB);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st) {
@@ -421,6 +536,51 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
       if (e == cudaSuccess)
         e = launch_sweep<3, 2, 16, 16, LAST>(M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
       if (e == cudaSuccess) e = launch_fallback<3>(M, q, g, dx, s.dt, Unew, Ufnew, st);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return e;
+}
+
+// Tile counts of a sweep of box dims along axis A (the item lists of a batch
+// enumerate these); must match the tile shapes the sweeps are launched with.
+void sweep_tiles(int ndim, int axis, const int* n, int* tS, int* tP) {
+  if (ndim == 1) {
+    *tS = 256;
+    *tP = 1;
+  } else if (axis == 0) {
+    *tS = 32;
+    *tP = 8;
+  } else {
+    *tS = 16;
+    *tP = 16;
+  }
+  (void)n;
+}
+
+// The mixed passes of one batch step after the CFL and ghost passes: the
+// sweeps of every box (slot 5 + axis of the queue heads), then the FP64
+// fix-up of the queued interfaces.
+cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const BatchLists& L,
+                                const FallbackQueue& q, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(q.n, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  switch (M.ndim) {
+    case 1:
+      e = launch_batch_sweep<1, 0, 256, 1, ONLY>(M, TB, L, q, 5, st);
+      if (e == cudaSuccess) e = launch_batch_fallback<1>(M, TB, q, st);
+      break;
+    case 2:
+      e = launch_batch_sweep<2, 0, 32, 8, FIRST>(M, TB, L, q, 5, st);
+      if (e == cudaSuccess) e = launch_batch_sweep<2, 1, 16, 16, LAST>(M, TB, L, q, 6, st);
+      if (e == cudaSuccess) e = launch_batch_fallback<2>(M, TB, q, st);
+      break;
+    case 3:
+      e = launch_batch_sweep<3, 0, 32, 8, FIRST>(M, TB, L, q, 5, st);
+      if (e == cudaSuccess) e = launch_batch_sweep<3, 1, 16, 16, MID>(M, TB, L, q, 6, st);
+      if (e == cudaSuccess) e = launch_batch_sweep<3, 2, 16, 16, LAST>(M, TB, L, q, 7, st);
+      if (e == cudaSuccess) e = launch_batch_fallback<3>(M, TB, q, st);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -39,6 +39,8 @@ struct MixedParams {
 struct FallbackEntry {
   int axis;
   int ga;
+  int box;  // index in the batch's box table (0 for a single box)
+  int pad;
   long long o;
   float l[5];
   float r[5];
@@ -120,6 +122,59 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   cudaStream_t st);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
+
+// ---- batches of boxes (kernels_batch.cu) ---------------------------------
+// One entry of a batch's device box table, for one step parity: U is read,
+// V written (and the FP32 mirrors Uf / Vf in mixed precision).
+struct BoxDesc {
+  double* U;
+  double* V;
+  float* Uf;
+  float* Vf;
+  float* acc;
+  double* faces;
+  double* fluxes;
+  double* ctl;  // control block: dt, CFL max bits, counter, status, ...
+  Geom g;
+  Dx dx;
+  double omega;
+  float omega_f;
+  int limiter;
+  int solver_type;
+  int bc[6];
+  double inflow[6][5];
+  int cfl_items;  // CFL work items of this box (last one finishes dt)
+};
+
+// A work item: `chunk` of pass `axis` of box `box` (or a sweep tile).
+struct WorkItem {
+  int box;
+  int axis;
+  long long chunk;
+};
+
+// Device views of a batch's per-pass item lists and queue heads.
+struct BatchLists {
+  const WorkItem* cfl;
+  const WorkItem* ghost;
+  const WorkItem* faces;
+  const WorkItem* flux;
+  const WorkItem* update;
+  const WorkItem* sweep[3];
+  int n_cfl, n_ghost, n_faces, n_flux, n_update, n_sweep[3];
+  int* heads;  // one queue head per pass (reset before each step)
+};
+
+void sweep_tiles(int ndim, int axis, const int* n, int* tS, int* tP);
+cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const BatchLists& L,
+                                const FallbackQueue& q, cudaStream_t st);
+cudaError_t launch_batch_step(const DevParams& P, const MixedParams& M, bool mixed, int ndim,
+                              const BoxDesc* table, const BatchLists& L, FallbackQueue q,
+                              cudaStream_t st);
+
+// Chunk sizes of the batched passes (elements per work item).
+constexpr int kBatchChunk = 256;
+constexpr int kBatchFluxChunk = 128;
 
 // Element-level launchers (kernels_elem.cu): device arrays in and out.
 cudaError_t launch_riemann_solve(const DevParams& P, const double* l, const double* r, long long n,

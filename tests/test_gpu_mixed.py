@@ -2,7 +2,9 @@
 accumulation, FP64 Riemann fallback) against the plain FP64 GPU path.
 
 Tolerance: relative L1 of the density <= 1e-6 after the stated steps (the
-bar the mixed form is quoted at); other fields <= 1e-5; dt within 1e-6.
+bar the mixed form is quoted at); total energy <= 1e-5; momentum components
+(which can be near zero everywhere) <= 1e-5 of the density's L1 norm times
+the box's maximum signal speed; dt within 1e-6.
 These workloads do not amplify rounding differences (the 2-D shear slab
 does, and is quoted in FP64 only).
 """
@@ -34,10 +36,16 @@ def check(p, cells, dx, nsteps, rho_tol=MIXED_L1_RHO, other_tol=MIXED_L1_OTHER):
     a, da, _ = run(p, cells, dx, nsteps, FP64)
     b, db, fb = run(p, cells, dx, nsteps, MIXED)
     assert np.isfinite(b).all()
-    errs = field_errors(b, a, p["ndim"])
+    nd = p["ndim"]
+    errs = field_errors(b, a, nd)
     assert errs[0][0] <= rho_tol, errs
-    for l1, _ in errs[1:]:
-        assert l1 <= other_tol, errs
+    assert errs[nd + 1][0] <= other_tol, errs
+    inner = (slice(None),) + (slice(2, -2),) * nd
+    ai, bi = a[inner], b[inner]
+    rho_norm = np.abs(ai[0]).sum()
+    vmax = max(np.abs(ai[1 + k] / ai[0]).max() for k in range(nd)) + np.sqrt(p["gamma"] * 10.0)
+    for k in range(nd):
+        assert np.abs(bi[1 + k] - ai[1 + k]).sum() <= other_tol * rho_norm * vmax, errs
     assert np.max(np.abs(db - da) / da) <= 1e-6
     return errs, fb
 
