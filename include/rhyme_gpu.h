@@ -227,6 +227,31 @@ int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params,
                                const int dims[3], const double dx[3], double dt,
                                void* stream);
 
+/* ---- batches of independent boxes -------------------------------------
+ * Steps many boxes of uneven sizes together, each with its own dt, boundary
+ * types, limiter and cell size, through one persistent kernel per pass fed
+ * by a work queue, one CUDA graph per step. Rhyme's driver steps only box 1
+ * of level 0 (rhyme_cfl_time_step.f90:42-49, rhyme_samr_bc_set_boundaries.f90:
+ * 9-20) and calls rhyme_muscl_hancock_solve once per box
+ * (src/main.f90:130-136); a batch runs that loop body for every box at once.
+ * A box stepped in a batch gives the same state and dt as stepped alone.
+ */
+typedef struct rhyme_gpu_batch rhyme_gpu_batch;
+
+/* Per-box boundary types (bc may be NULL to keep the context's), limiter id
+ * and omega, overriding the context's for this box in every call. */
+int rhyme_gpu_set_box_params(rhyme_gpu_ctx* ctx, int handle, const int bc[6],
+                             int limiter, double omega);
+
+/* A batch of n registered boxes; dx[3*i .. 3*i+2] is box i's cell size. */
+int rhyme_gpu_batch_create(rhyme_gpu_ctx* ctx, const int* handles,
+                           const double* dx, int n, rhyme_gpu_batch** batch);
+/* nsteps driver steps of every box of the batch (asynchronous). */
+int rhyme_gpu_batch_run(rhyme_gpu_batch* batch, int nsteps);
+/* dts[i] = the dt of box i's last step (waits for the stream). */
+int rhyme_gpu_batch_dt(rhyme_gpu_batch* batch, double* dts);
+int rhyme_gpu_batch_destroy(rhyme_gpu_batch* batch);
+
 /* Waits (bounded) for all work on the context stream. */
 int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);
 

@@ -43,6 +43,9 @@ struct Box {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   Dx graph_dx{};
   bool graph_valid = false;
+  DevParams dp{};   // the context's parameters with this box's overrides
+  MixedParams mp{};
+  Dx dx{};          // cell size for batched steps (rhyme_gpu_batch_create)
 };
 
 }  // namespace
@@ -296,6 +299,8 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
     if (a >= D && dims[a] != 1) return fail(ctx, RHYME_GPU_EINVAL, "dims(%d) must be 1 beyond NDIM", a + 1);
   }
   Box* b = new Box();
+  b->dp = ctx->dp;
+  b->mp = ctx->mp;
   b->level = level;
   b->number = number;
   b->host = cells;
@@ -420,17 +425,17 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
   double* U = b->state[cur];
   double* V = b->state[1 - cur];
   if (ctx->mixed) {
-    cudaError_t e = launch_cfl_mixed(ctx->mp, b->Uf[cur], b->g, ctx->dp.courant, dx, s, ctx->stream);
-    if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
-    if (e == cudaSuccess) e = launch_ghost_fill_f32(ctx->dp, b->Uf[cur], b->g, ctx->stream);
+    cudaError_t e = launch_cfl_mixed(b->mp, b->Uf[cur], b->g, b->dp.courant, dx, s, ctx->stream);
+    if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
+    if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[cur], b->g, ctx->stream);
     if (e == cudaSuccess)
-      e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fbq,
+      e = launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fbq,
                                 ctx->stream);
     return e;
   }
-  cudaError_t e = launch_cfl(ctx->dp, U, b->g, dx, s, ctx->stream);
-  if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
-  if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, dx, s, ctx->stream);
+  cudaError_t e = launch_cfl(b->dp, U, b->g, dx, s, ctx->stream);
+  if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
+  if (e == cudaSuccess) e = launch_mh_solve(b->dp, U, V, b->g, dx, s, ctx->stream);
   return e;
 }
 
@@ -471,9 +476,9 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], 
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   Dx d = make_dx(ctx->params.ndim, dx);
   if (ctx->mixed)
-    CK(launch_cfl_mixed(ctx->mp, b->Uf[b->cur], b->g, ctx->dp.courant, d, scratch_of(b, false), ctx->stream));
+    CK(launch_cfl_mixed(b->mp, b->Uf[b->cur], b->g, b->dp.courant, d, scratch_of(b, false), ctx->stream));
   else
-    CK(launch_cfl(ctx->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
+    CK(launch_cfl(b->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
   CK(cudaMemcpyAsync(ctx->pinned_dt, b->s.dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   int rc = wait_stream(ctx);
   if (rc != RHYME_GPU_OK) return rc;
@@ -491,8 +496,8 @@ int rhyme_gpu_set_boundaries(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
-  CK(launch_ghost_fill(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, ctx->stream));
-  if (ctx->mixed) CK(launch_ghost_fill_f32(ctx->dp, b->Uf[b->cur], b->g, ctx->stream));
+  CK(launch_ghost_fill(b->dp, b->state[b->cur], b->state[1 - b->cur], b->g, ctx->stream));
+  if (ctx->mixed) CK(launch_ghost_fill_f32(b->dp, b->Uf[b->cur], b->g, ctx->stream));
   return RHYME_GPU_OK;
 }
 
@@ -509,10 +514,10 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   ctx->pinned_dt[0] = dt;
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->mixed)
-    CK(launch_mh_solve_mixed(ctx->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
+    CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
                              b->acc, b->g, d, scratch_of(b, false), b->fbq, ctx->stream));
   else
-    CK(launch_mh_solve(ctx->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
+    CK(launch_mh_solve(b->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
                        ctx->stream));
   b->cur = 1 - b->cur;
   return RHYME_GPU_OK;
@@ -675,22 +680,22 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
     cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
     if (ctx->mixed) {
       // mixed: the fused sweeps are reported under "fluxes"
-      if (e == cudaSuccess) e = launch_cfl_mixed(ctx->mp, b->Uf[b->cur], b->g, ctx->dp.courant, d, sc, ctx->stream);
+      if (e == cudaSuccess) e = launch_cfl_mixed(b->mp, b->Uf[b->cur], b->g, b->dp.courant, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
-      if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
-      if (e == cudaSuccess) e = launch_ghost_fill_f32(ctx->dp, b->Uf[b->cur], b->g, ctx->stream);
+      if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
+      if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[b->cur], b->g, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[3], ctx->stream);
       if (e == cudaSuccess)
-        e = launch_mh_solve_mixed(ctx->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
+        e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
                                   b->fbq, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[4], ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[5], ctx->stream);
     } else {
-      if (e == cudaSuccess) e = launch_cfl(ctx->dp, U, b->g, d, sc, ctx->stream);
+      if (e == cudaSuccess) e = launch_cfl(b->dp, U, b->g, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
-      if (e == cudaSuccess) e = launch_ghost_fill(ctx->dp, U, V, b->g, ctx->stream);
-      if (e == cudaSuccess) e = launch_mh_solve(ctx->dp, U, V, b->g, d, sc, ctx->stream, ev + 2);
+      if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
+      if (e == cudaSuccess) e = launch_mh_solve(b->dp, U, V, b->g, d, sc, ctx->stream, ev + 2);
     }
     if (e != cudaSuccess) {
       rc = fail(ctx, RHYME_GPU_ECUDA, "profile launch: %s", cudaGetErrorString(e));
@@ -720,5 +725,275 @@ extern "C" int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long lon
   int rc = wait_stream(ctx);
   if (rc != RHYME_GPU_OK) return rc;
   *count = *st;
+  return RHYME_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Per-box parameters and batches of boxes
+// ---------------------------------------------------------------------------
+extern "C" int rhyme_gpu_set_box_params(rhyme_gpu_ctx* ctx, int handle, const int bc[6], int limiter,
+                                        double omega) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  const int D = ctx->params.ndim;
+  if (limiter < 1 || limiter > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown slope limiter %d", limiter);
+  if (bc)
+    for (int i = 0; i < 2 * D; ++i)
+      if (bc[i] < 1 || bc[i] > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d", bc[i]);
+  if (bc)
+    for (int i = 0; i < 2 * D; ++i) b->dp.bc[i] = bc[i];
+  b->dp.limiter = limiter;
+  b->dp.omega = omega;
+  b->mp.limiter = limiter;
+  b->mp.omega = (float)omega;
+  b->graph_valid = false;
+  return RHYME_GPU_OK;
+}
+
+struct rhyme_gpu_batch {
+  rhyme_gpu_ctx* ctx = nullptr;
+  std::vector<int> handles;
+  std::vector<int> base_cur;  // box parity when the tables were built
+  int k = 0;                  // steps taken since (mod 2)
+  BoxDesc* table[2] = {nullptr, nullptr};
+  WorkItem* items = nullptr;
+  int* heads = nullptr;
+  BatchLists L{};
+  FallbackQueue q{};
+  int* qblock = nullptr;  // n, status, total
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+void batch_free(rhyme_gpu_batch* B) {
+  for (int p = 0; p < 2; ++p) {
+    if (B->graph[p]) cudaGraphExecDestroy(B->graph[p]);
+    B->graph[p] = nullptr;
+    cudaFree(B->table[p]);
+    B->table[p] = nullptr;
+  }
+  cudaFree(B->items);
+  cudaFree(B->heads);
+  cudaFree(B->q.e);
+  cudaFree(B->qblock);
+  B->items = nullptr;
+  B->heads = nullptr;
+  B->q.e = nullptr;
+  B->qblock = nullptr;
+}
+
+// Builds the box tables (both parities), the work-item lists and the
+// per-parity step graphs.
+int batch_build(rhyme_gpu_batch* B) {
+  rhyme_gpu_ctx* ctx = B->ctx;
+  const int D = ctx->params.ndim;
+  const int n = (int)B->handles.size();
+  batch_free(B);
+  B->base_cur.resize(n);
+  B->k = 0;
+  // order: largest boxes first (the queues hand them out first)
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  auto cells_of = [&](int i) {
+    const Box* b = ctx->boxes[B->handles[i]];
+    return (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cells_of(a) > cells_of(c); });
+
+  std::vector<BoxDesc> tab[2];
+  tab[0].resize(n);
+  tab[1].resize(n);
+  std::vector<WorkItem> cfl, ghost, faces, flux, update, sweep[3];
+  long long qcap = 0;
+  for (int i = 0; i < n; ++i) {
+    Box* b = ctx->boxes[B->handles[i]];
+    B->base_cur[i] = b->cur;
+    const long long cells = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+    qcap += D * cells / 16;
+    for (int p = 0; p < 2; ++p) {
+      BoxDesc& d = tab[p][i];
+      memset(&d, 0, sizeof(d));
+      const int c = b->cur ^ p;
+      d.U = b->state[c];
+      d.V = b->state[1 - c];
+      d.Uf = b->Uf[c];
+      d.Vf = b->Uf[1 - c];
+      d.acc = b->acc;
+      d.faces = b->s.faces;
+      d.fluxes = b->s.fluxes;
+      d.ctl = b->s.dt;
+      d.g = b->g;
+      d.dx = b->dx;
+      d.omega = b->dp.omega;
+      d.omega_f = (float)b->dp.omega;
+      d.limiter = b->dp.limiter;
+      d.solver_type = b->dp.solver_type;
+      for (int f = 0; f < 6; ++f) {
+        d.bc[f] = b->dp.bc[f];
+        for (int cc = 0; cc < 5; ++cc) d.inflow[f][cc] = b->dp.inflow[f][cc];
+      }
+      d.cfl_items = (int)((cells + kBatchChunk - 1) / kBatchChunk);
+    }
+  }
+  for (int oi = 0; oi < n; ++oi) {
+    const int i = order[oi];
+    const Box* b = ctx->boxes[B->handles[i]];
+    const Geom& g = b->g;
+    const long long cells = (long long)g.n[0] * g.n[1] * g.n[2];
+    for (long long c = 0; c * kBatchChunk < cells; ++c) cfl.push_back({i, 0, c});
+    long long lines = 0;
+    for (int a = 0; a < D; ++a) {
+      long long t = D + 2;
+      for (int o = 0; o < D; ++o)
+        if (o != a) t *= g.n[o];
+      lines += t;
+    }
+    for (long long c = 0; c * kBatchChunk < lines; ++c) ghost.push_back({i, 0, c});
+    if (ctx->mixed) {
+      for (int a = 0; a < D; ++a) {
+        int S, P;
+        sweep_tiles(D, a, g.n, &S, &P);
+        const int bax = (D == 1) ? 1 : (a == 0 ? 1 : 0);
+        const int cax = (D == 3) ? 3 - a - bax : 2;
+        const long long nA = (g.n[a] + S - 1) / S;
+        const long long nB = ((bax < D ? g.n[bax] : 1) + P - 1) / P;
+        const long long nC = (cax < D) ? g.n[cax] : 1;
+        for (long long t = 0; t < nA * nB * nC; ++t) sweep[a].push_back({i, a, t});
+      }
+    } else {
+      for (int a = 0; a < D; ++a) {
+        long long fc = 1, ic = 1;
+        for (int o = 0; o < 3; ++o) {
+          fc *= (o == a) ? g.n[o] + 2 : g.n[o];
+          ic *= (o == a) ? g.n[o] + 1 : g.n[o];
+        }
+        for (long long c = 0; c * kBatchFluxChunk < fc; ++c) faces.push_back({i, a, c});
+        for (long long c = 0; c * kBatchFluxChunk < ic; ++c) flux.push_back({i, a, c});
+      }
+      for (long long c = 0; c * kBatchChunk < cells; ++c) update.push_back({i, 0, c});
+    }
+  }
+  std::vector<WorkItem> all;
+  size_t off[8];
+  std::vector<WorkItem>* lists[8] = {&cfl, &ghost, &faces, &flux, &update, &sweep[0], &sweep[1], &sweep[2]};
+  for (int k = 0; k < 8; ++k) {
+    off[k] = all.size();
+    all.insert(all.end(), lists[k]->begin(), lists[k]->end());
+  }
+  for (int p = 0; p < 2; ++p) {
+    CK(cudaMalloc(&B->table[p], sizeof(BoxDesc) * std::max(n, 1)));
+    CK(cudaMemcpyAsync(B->table[p], tab[p].data(), sizeof(BoxDesc) * n, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaMalloc(&B->items, sizeof(WorkItem) * std::max<size_t>(all.size(), 1)));
+  CK(cudaMemcpyAsync(B->items, all.data(), sizeof(WorkItem) * all.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMalloc(&B->heads, 16 * sizeof(int)));
+  CK(cudaMalloc(&B->qblock, 16 * sizeof(int)));
+  CK(cudaMemsetAsync(B->qblock, 0, 16 * sizeof(int), ctx->stream));
+  B->q.cap = 0;
+  if (ctx->mixed) {
+    B->q.cap = (int)std::min<long long>(std::max<long long>(65536, qcap), 1LL << 30);
+    CK(cudaMalloc(&B->q.e, sizeof(FallbackEntry) * (size_t)B->q.cap));
+  }
+  B->q.n = B->qblock + 0;
+  B->q.status = B->qblock + 1;
+  B->q.total = B->qblock + 2;
+  BatchLists& L = B->L;
+  L.cfl = B->items + off[0];
+  L.ghost = B->items + off[1];
+  L.faces = B->items + off[2];
+  L.flux = B->items + off[3];
+  L.update = B->items + off[4];
+  for (int a = 0; a < 3; ++a) L.sweep[a] = B->items + off[5 + a];
+  L.n_cfl = (int)cfl.size();
+  L.n_ghost = (int)ghost.size();
+  L.n_faces = (int)faces.size();
+  L.n_flux = (int)flux.size();
+  L.n_update = (int)update.size();
+  for (int a = 0; a < 3; ++a) L.n_sweep[a] = (int)sweep[a].size();
+  L.heads = B->heads;
+  // one step per parity, captured
+  for (int p = 0; p < 2; ++p) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_batch_step(ctx->dp, ctx->mp, ctx->mixed, D, B->table[p], L, B->q, ctx->stream);
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (e2 == cudaSuccess) cudaGraphDestroy(graph);
+      return fail(ctx, RHYME_GPU_ECUDA, "batch graph capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&B->graph[p], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e3 != cudaSuccess) return fail(ctx, RHYME_GPU_ECUDA, "batch graph instantiate: %s", cudaGetErrorString(e3));
+  }
+  return RHYME_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int rhyme_gpu_batch_create(rhyme_gpu_ctx* ctx, const int* handles, const double* dx, int n,
+                                      rhyme_gpu_batch** out) {
+  if (!ctx || !handles || !dx || !out || n < 1) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  *out = nullptr;
+  const int D = ctx->params.ndim;
+  for (int i = 0; i < n; ++i) {
+    Box* b = find_box(ctx, handles[i]);
+    if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handles[i]);
+    for (int j = 0; j < i; ++j)
+      if (handles[j] == handles[i]) return fail(ctx, RHYME_GPU_EINVAL, "box handle %d listed twice", handles[i]);
+    for (int a = 0; a < D; ++a)
+      if (!(dx[3 * i + a] > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "dx of box %d must be positive", handles[i]);
+    b->dx = make_dx(D, dx + 3 * i);
+  }
+  rhyme_gpu_batch* B = new rhyme_gpu_batch();
+  B->ctx = ctx;
+  B->handles.assign(handles, handles + n);
+  int rc = batch_build(B);
+  if (rc != RHYME_GPU_OK) {
+    batch_free(B);
+    delete B;
+    return rc;
+  }
+  *out = B;
+  return RHYME_GPU_OK;
+}
+
+extern "C" int rhyme_gpu_batch_run(rhyme_gpu_batch* B, int nsteps) {
+  if (!B) return RHYME_GPU_EINVAL;
+  rhyme_gpu_ctx* ctx = B->ctx;
+  if (nsteps < 0) return fail(ctx, RHYME_GPU_EINVAL, "nsteps must be >= 0");
+  // rebuild if a box was stepped on its own since the tables were built
+  for (size_t i = 0; i < B->handles.size(); ++i) {
+    Box* b = find_box(ctx, B->handles[i]);
+    if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "box %d of the batch was unregistered", B->handles[i]);
+    if (b->cur != (B->base_cur[i] ^ B->k)) {
+      int rc = batch_build(B);
+      if (rc != RHYME_GPU_OK) return rc;
+      break;
+    }
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    CK(cudaGraphLaunch(B->graph[B->k], ctx->stream));
+    B->k ^= 1;
+  }
+  for (size_t i = 0; i < B->handles.size(); ++i) ctx->boxes[B->handles[i]]->cur = B->base_cur[i] ^ B->k;
+  return RHYME_GPU_OK;
+}
+
+extern "C" int rhyme_gpu_batch_dt(rhyme_gpu_batch* B, double* dts) {
+  if (!B || !dts) return RHYME_GPU_EINVAL;
+  rhyme_gpu_ctx* ctx = B->ctx;
+  for (size_t i = 0; i < B->handles.size(); ++i)
+    CK(cudaMemcpyAsync(dts + i, ctx->boxes[B->handles[i]]->s.dt, sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  return wait_stream(ctx);
+}
+
+extern "C" int rhyme_gpu_batch_destroy(rhyme_gpu_batch* B) {
+  if (!B) return RHYME_GPU_OK;
+  cudaStreamSynchronize(B->ctx->stream);
+  batch_free(B);
+  delete B;
   return RHYME_GPU_OK;
 }

@@ -31,7 +31,8 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
-           "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc"]
+           "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc", "rhyme_gpu_set_box_params",
+           "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy"]
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 
 
@@ -112,6 +113,11 @@ def load():
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     L.rhyme_gpu_mh_solve_noalloc.argtypes = [C.POINTER(Params), vp, vp, ip, dp, C.c_double, vp]
+    L.rhyme_gpu_set_box_params.argtypes = [vp, C.c_int, ip, C.c_int, C.c_double]
+    L.rhyme_gpu_batch_create.argtypes = [vp, ip, dp, C.c_int, C.POINTER(vp)]
+    L.rhyme_gpu_batch_run.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_batch_dt.argtypes = [vp, dp]
+    L.rhyme_gpu_batch_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -133,6 +139,42 @@ def _dx3(dx):
 class Box:
     def __init__(self, ctx, handle, cells, dims):
         self.ctx, self.handle, self.cells, self.dims = ctx, handle, cells, dims
+
+
+class Batch:
+    """rhyme_gpu_batch: independent boxes stepped together (own dt each)."""
+
+    def __init__(self, ctx, boxes, dxs):
+        self.ctx = ctx
+        self.boxes = list(boxes)
+        n = len(self.boxes)
+        handles = np.array([b.handle for b in self.boxes], dtype=np.int32)
+        dx = np.ones((n, 3))
+        for i, d in enumerate(dxs):
+            dx[i, :len(d)] = d
+        h = C.c_void_p()
+        ctx._check(ctx.lib.rhyme_gpu_batch_create(ctx.h, handles.ctypes.data_as(C.POINTER(C.c_int)),
+                                                   _d(dx), n, C.byref(h)))
+        self.h = h
+
+    def run(self, nsteps):
+        self.ctx._check(self.ctx.lib.rhyme_gpu_batch_run(self.h, int(nsteps)))
+
+    def dts(self):
+        out = np.zeros(len(self.boxes))
+        self.ctx._check(self.ctx.lib.rhyme_gpu_batch_dt(self.h, _d(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.rhyme_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Context:
@@ -219,6 +261,22 @@ class Context:
 
     def synchronize(self):
         self._check(self.lib.rhyme_gpu_synchronize(self.h))
+
+    def set_box_params(self, box, bc=None, limiter=None, omega=None):
+        """Per-box boundary types / limiter / omega (defaults: the context's)."""
+        limiter = self.params["limiter"] if limiter is None else limiter
+        omega = self.params.get("omega", 0.0) if omega is None else omega
+        bcs = None
+        if bc is not None:
+            bcs = np.zeros(6, dtype=np.int32)
+            bcs[:len(bc)] = bc
+        self._check(self.lib.rhyme_gpu_set_box_params(
+            self.h, box.handle, bcs.ctypes.data_as(C.POINTER(C.c_int)) if bcs is not None else None,
+            int(limiter), float(omega)))
+
+    def batch(self, boxes, dxs):
+        """A Batch stepping `boxes` together (dxs: one cell size per box)."""
+        return Batch(self, boxes, dxs)
 
     # ---- the driver's step ---------------------------------------------
     def cfl_time_step(self, box, dx):
