@@ -252,6 +252,49 @@ int rhyme_gpu_batch_run(rhyme_gpu_batch* batch, int nsteps);
 int rhyme_gpu_batch_dt(rhyme_gpu_batch* batch, double* dts);
 int rhyme_gpu_batch_destroy(rhyme_gpu_batch* batch);
 
+/* ---- serving: continuous batching of hydro solves (no reference
+ * counterpart; the reference runs one solve per process) ------------------
+ * Requests of any dimensionality and size are submitted as they arrive;
+ * each tick admits pending requests first come first served while the HBM
+ * budget and the active-request cap allow, advances every active request by
+ * one step (one batch per dimensionality, each on its own stream, so their
+ * work overlaps on the device) and retires finished ones: their state is
+ * downloaded asynchronously on a copy stream through page-locked staging and
+ * copied into the request's cells array when the copy completes.
+ */
+enum { RHYME_GPU_REQ_PENDING = 0, RHYME_GPU_REQ_ACTIVE = 1,
+       RHYME_GPU_REQ_DRAINING = 2, RHYME_GPU_REQ_DONE = 3 };
+
+typedef struct rhyme_gpu_request {
+  int ndim;
+  int dims[3];
+  int nsteps;
+  int limiter;
+  int bc[6];
+  double omega;
+  double dx[3];
+  double* cells;  /* host, NDIM+2 ghosted blocks: initial state in, result out */
+} rhyme_gpu_request;
+
+typedef struct rhyme_gpu_server rhyme_gpu_server;
+
+/* base: gas, Riemann, precision (ndim, limiter, bc ignored); courant[k] is
+ * the Courant number of (k+1)-D requests. */
+int rhyme_gpu_server_create(const rhyme_gpu_params* base, const double courant[3],
+                            long long hbm_budget_bytes, int max_active,
+                            rhyme_gpu_server** server);
+int rhyme_gpu_server_submit(rhyme_gpu_server* server, const rhyme_gpu_request* req, int* id);
+int rhyme_gpu_server_tick(rhyme_gpu_server* server, int* n_active, int* n_pending,
+                          int* n_draining);
+/* state (RHYME_GPU_REQ_*), times = (submitted, admitted, done) in seconds
+ * since the server started, steps taken. */
+int rhyme_gpu_server_request(rhyme_gpu_server* server, int id, int* state, double times[3],
+                             int* steps_done);
+int rhyme_gpu_server_stats(rhyme_gpu_server* server, long long* cell_updates,
+                           long long* hbm_used);
+const char* rhyme_gpu_server_last_error(const rhyme_gpu_server* server);
+int rhyme_gpu_server_destroy(rhyme_gpu_server* server);
+
 /* Waits (bounded) for all work on the context stream. */
 int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx);
 

@@ -176,7 +176,12 @@ cudaError_t batch_step_d(const DevParams& P, const MixedParams& M, bool mixed, c
   // queue heads: 0 cfl, 1 ghost, 2 faces, 3 flux, 4 update, 5..7 sweeps, 8 ghost f32
   cudaError_t e = cudaMemsetAsync(L.heads, 0, 16 * sizeof(int), st);
   if (e != cudaSuccess) return e;
-  if (L.n_cfl) batch_cfl_kernel<D><<<152 * 4, 256, 0, st>>>(P.G, P.courant, TB, L.cfl, L.n_cfl, L.heads + 0);
+  if (mixed) {
+    e = launch_batch_cfl_mixed(M, P.courant, TB, L, st);
+    if (e != cudaSuccess) return e;
+  } else if (L.n_cfl) {
+    batch_cfl_kernel<D><<<152 * 4, 256, 0, st>>>(P.G, P.courant, TB, L.cfl, L.n_cfl, L.heads + 0);
+  }
   if (L.n_ghost) {
     batch_ghost_kernel<D, double><<<152 * 4, 256, 0, st>>>(TB, L.ghost, L.n_ghost, L.heads + 1, false);
     if (mixed) batch_ghost_kernel<D, float><<<152 * 4, 256, 0, st>>>(TB, L.ghost, L.n_ghost, L.heads + 8, true);

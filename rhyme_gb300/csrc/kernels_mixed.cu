@@ -46,32 +46,41 @@ __global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restri
     Uf[t] = (float)U[t];
 }
 
+// |v| + cs of interior cell t of Uf in FP32; bad marks non-positive density
+// or a non-finite value.
+template <int D>
+__device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const float* __restrict__ Uf,
+                                                  const Geom& g, long long t, int& bad) {
+  const long long n0 = g.n[0], n1 = g.n[1];
+  const int i = (int)(t % n0) + 1;
+  const long long q = t / n0;
+  const int j = (int)(q % n1) + 1;
+  const int k = (int)(q / n1) + 1;
+  const long long o = g.at(D, i, j, k);
+  float u[D + 2];
+#pragma unroll
+  for (int c = 0; c < D + 2; ++c) u[c] = Uf[(long long)c * g.field + o];
+  float ss = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
+  const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
+  if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
+  return v;
+}
+
 // FP32 signal-speed maximum over the interior of Uf; the last block forms
 // dt = courant * min(dx) / max in FP64 and resets the accumulators.
 template <int D>
 __global__ void __launch_bounds__(kThreads)
     cfl_f32_kernel(MixedParams M, const float* __restrict__ Uf, Geom g, double courant, double mdx,
                    StepScratch s) {
-  const long long n0 = g.n[0], n1 = g.n[1];
-  const long long total = n0 * n1 * (long long)g.n[2];
+  const long long total = (long long)g.n[0] * g.n[1] * (long long)g.n[2];
   float m = 0.f;
   int bad = 0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % n0) + 1;
-    const long long q = t / n0;
-    const int j = (int)(q % n1) + 1;
-    const int k = (int)(q / n1) + 1;
-    const long long o = g.at(D, i, j, k);
-    float u[D + 2];
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) u[c] = Uf[(long long)c * g.field + o];
-    float ss = 0.f;
-#pragma unroll
-    for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
-    const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
+    const float v = signal_speed_f32<D>(M, Uf, g, t, bad);
     if (v > m) m = v;
-    if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -420,6 +429,65 @@ cudaError_t launch_fallback(const MixedParams& M, const FallbackQueue& q, const 
   return cudaGetLastError();
 }
 
+// Batched FP32 CFL over work items (chunks of 256 cells of a box): per-box
+// maximum through atomics, the last item of a box forms its dt in FP64.
+template <int D>
+__global__ void __launch_bounds__(256)
+    batch_cfl_f32_kernel(MixedParams M, double courant, const BoxDesc* __restrict__ TB,
+                         const WorkItem* __restrict__ items, int n, int* head) {
+  __shared__ float sm[8];
+  __shared__ int sb[8];
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n) break;
+    const WorkItem w = items[it];
+    const BoxDesc& b = TB[w.box];
+    const long long total = (long long)b.g.n[0] * b.g.n[1] * b.g.n[2];
+    const long long t = w.chunk * kBatchChunk + threadIdx.x;
+    float m = 0.f;
+    int bad = 0;
+    if (t < total) {
+      const float v = signal_speed_f32<D>(M, b.Uf, b.g, t, bad);
+      if (v > m) m = v;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float o = __shfl_down_sync(0xffffffffu, m, off);
+      if (o > m) m = o;
+      bad |= __shfl_down_sync(0xffffffffu, bad, off);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+      sm[warp] = m;
+      sb[warp] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < 8; ++k) {
+        if (sm[k] > m) m = sm[k];
+        bad |= sb[k];
+      }
+      unsigned long long* max_bits = (unsigned long long*)(b.ctl + 1);
+      unsigned int* counter = (unsigned int*)(b.ctl + 2);
+      int* status = (int*)(b.ctl + 2) + 1;
+      atomicMax(max_bits, (unsigned long long)__float_as_uint(m));
+      if (bad) atomicOr(status, 1);
+      __threadfence();
+      if (atomicAdd(counter, 1u) == (unsigned int)(b.cfl_items - 1)) {
+        __threadfence();
+        const float mu = __uint_as_float((unsigned int)atomicAdd(max_bits, 0ull));
+        b.ctl[0] = courant * b.dx.min / (double)mu;
+        atomicExch(max_bits, 0ull);
+        atomicExch(counter, 0u);
+      }
+    }
+  }
+}
+
 // Batched FP64 fix-up: as fallback_fix_kernel, with the box of each entry.
 template <int D>
 __global__ void __launch_bounds__(128)
@@ -557,6 +625,18 @@ void sweep_tiles(int ndim, int axis, const int* n, int* tS, int* tP) {
     *tP = 16;
   }
   (void)n;
+}
+
+cudaError_t launch_batch_cfl_mixed(const MixedParams& M, double courant, const BoxDesc* TB,
+                                   const BatchLists& L, cudaStream_t st) {
+  if (!L.n_cfl) return cudaSuccess;
+  switch (M.ndim) {
+    case 1: batch_cfl_f32_kernel<1><<<152 * 4, 256, 0, st>>>(M, courant, TB, L.cfl, L.n_cfl, L.heads + 0); break;
+    case 2: batch_cfl_f32_kernel<2><<<152 * 4, 256, 0, st>>>(M, courant, TB, L.cfl, L.n_cfl, L.heads + 0); break;
+    case 3: batch_cfl_f32_kernel<3><<<152 * 4, 256, 0, st>>>(M, courant, TB, L.cfl, L.n_cfl, L.heads + 0); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 // The mixed passes of one batch step after the CFL and ghost passes: the

@@ -166,6 +166,8 @@ struct BatchLists {
 };
 
 void sweep_tiles(int ndim, int axis, const int* n, int* tS, int* tP);
+cudaError_t launch_batch_cfl_mixed(const MixedParams& M, double courant, const BoxDesc* TB,
+                                   const BatchLists& L, cudaStream_t st);
 cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const BatchLists& L,
                                 const FallbackQueue& q, cudaStream_t st);
 cudaError_t launch_batch_step(const DevParams& P, const MixedParams& M, bool mixed, int ndim,

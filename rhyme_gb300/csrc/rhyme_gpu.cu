@@ -40,6 +40,7 @@ struct Box {
   double* trace_buf = nullptr;
   int* trace_pos = nullptr;
   bool registered_host = false;
+  bool host_pinned = false;  // host array is page-locked (no wait after upload)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   Dx graph_dx{};
   bool graph_valid = false;
@@ -203,18 +204,20 @@ void make_mixed_params(const DevParams& d, MixedParams* m) {
   m->omega = (float)d.omega;
 }
 
-void destroy_box(Box* b) {
+// Frees a box's device memory in stream order on `st` (after the work
+// already queued there) and unpins the caller's array.
+void destroy_box(Box* b, cudaStream_t st) {
   if (!b) return;
   for (int i = 0; i < 2; ++i) {
     if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
-    cudaFree(b->state[i]);
-    cudaFree(b->Uf[i]);
+    if (b->state[i]) cudaFreeAsync(b->state[i], st);
+    if (b->Uf[i]) cudaFreeAsync(b->Uf[i], st);
   }
-  cudaFree(b->acc);
-  cudaFree(b->fbq.e);
-  cudaFree(b->s.faces);
-  cudaFree(b->s.fluxes);
-  cudaFree(b->s.dt);
+  if (b->acc) cudaFreeAsync(b->acc, st);
+  if (b->fbq.e) cudaFreeAsync(b->fbq.e, st);
+  if (b->s.faces) cudaFreeAsync(b->s.faces, st);
+  if (b->s.fluxes) cudaFreeAsync(b->s.fluxes, st);
+  if (b->s.dt) cudaFreeAsync(b->s.dt, st);
   if (b->registered_host) cudaHostUnregister(b->host);
   delete b;
 }
@@ -267,7 +270,8 @@ int rhyme_gpu_create(rhyme_gpu_ctx** out, const rhyme_gpu_params* params) {
 int rhyme_gpu_destroy(rhyme_gpu_ctx* ctx) {
   if (!ctx) return RHYME_GPU_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (Box* b : ctx->boxes) destroy_box(b);
+  for (Box* b : ctx->boxes) destroy_box(b, ctx->stream);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->elem_buf);
   cudaFreeHost(ctx->pinned_dt);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -288,8 +292,27 @@ int rhyme_gpu_synchronize(rhyme_gpu_ctx* ctx) {
   return wait_stream(ctx);
 }
 
-int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* cells,
-                           const int dims[3], int ghost, int ncmp, int* handle) {
+}  // extern "C"
+
+namespace {
+
+// Device bytes a box of these dims takes (state buffers and scratch).
+long long box_device_bytes(int D, bool mixed, const int* dims) {
+  const Geom g = make_geom(D, dims);
+  const long long F = g.field;
+  long long bytes = 2LL * (D + 2) * F * 8 + 64 + 8 * kTraceCap;
+  if (mixed) {
+    const long long cells = (long long)g.n[0] * g.n[1] * g.n[2];
+    bytes += 2LL * (D + 2) * F * 4 + (D > 1 ? (D + 2) * F * 4 : 0);
+    bytes += std::max<long long>(4096, D * cells / 16) * (long long)sizeof(FallbackEntry);
+  } else {
+    bytes += 3LL * D * (D + 2) * F * 8;
+  }
+  return bytes;
+}
+
+int register_box_impl(rhyme_gpu_ctx* ctx, int level, int number, double* cells, const int dims[3], int ghost,
+                      int ncmp, bool pin, bool upload, int* handle, bool host_pinned = false) {
   if (!ctx || !cells || !dims || !handle) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
   const int D = ctx->params.ndim;
   if (ghost != 2) return fail(ctx, RHYME_GPU_EINVAL, "ghost width must be 2 (got %d)", ghost);
@@ -304,29 +327,33 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   b->level = level;
   b->number = number;
   b->host = cells;
+  b->host_pinned = host_pinned;
   b->ncmp = ncmp;
   for (int a = 0; a < 3; ++a) b->dims[a] = dims[a];
   b->g = make_geom(D, dims);
   const long long F = b->g.field;
   b->hydro_bytes = (size_t)(D + 2) * F * sizeof(double);
+  cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->state[i], b->hydro_bytes);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMallocAsync((void**)&b->state[i], b->hydro_bytes, st);
   if (ctx->mixed) {
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&b->Uf[i], (size_t)(D + 2) * F * sizeof(float));
-    if (e == cudaSuccess && D > 1) e = cudaMalloc(&b->acc, (size_t)(D + 2) * F * sizeof(float));
-    long long cells = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
-    b->fbq.cap = (int)std::min<long long>(std::max<long long>(4096, D * cells / 16), 1LL << 30);
-    if (e == cudaSuccess) e = cudaMalloc(&b->fbq.e, (size_t)b->fbq.cap * sizeof(FallbackEntry));
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+      e = cudaMallocAsync((void**)&b->Uf[i], (size_t)(D + 2) * F * sizeof(float), st);
+    if (e == cudaSuccess && D > 1) e = cudaMallocAsync((void**)&b->acc, (size_t)(D + 2) * F * sizeof(float), st);
+    long long cells_n = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+    b->fbq.cap = (int)std::min<long long>(std::max<long long>(4096, D * cells_n / 16), 1LL << 30);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->fbq.e, (size_t)b->fbq.cap * sizeof(FallbackEntry), st);
   } else {
-    if (e == cudaSuccess) e = cudaMalloc(&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double));
+    if (e == cudaSuccess)
+      e = cudaMallocAsync((void**)&b->s.faces, (size_t)2 * D * (D + 2) * F * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->s.fluxes, (size_t)D * (D + 2) * F * sizeof(double), st);
   }
   // small block: dt, max_bits, counter, status, trace_pos, then the trace
   const size_t small = 64 + sizeof(double) * kTraceCap;
-  if (e == cudaSuccess) e = cudaMalloc(&b->s.dt, small);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->s.dt, 0, small, ctx->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->s.dt, small, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->s.dt, 0, small, st);
   if (e != cudaSuccess) {
-    destroy_box(b);
+    destroy_box(b, st);
     return fail(ctx, e == cudaErrorMemoryAllocation ? RHYME_GPU_ENOMEM : RHYME_GPU_ECUDA,
                 "box allocation: %s", cudaGetErrorString(e));
   }
@@ -340,23 +367,47 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* ce
   b->fbq.status = b->s.status;
   b->fbq.total = b->fb_count;
   b->trace_buf = (double*)(base + 64);
-  // Pin the caller's array for asynchronous copies when possible; a failure
-  // here only costs copy speed.
-  if (cudaHostRegister(cells, (size_t)ncmp * F * sizeof(double), cudaHostRegisterDefault) == cudaSuccess)
-    b->registered_host = true;
-  else
-    cudaGetLastError();
-  ctx->boxes.push_back(b);
-  *handle = (int)ctx->boxes.size() - 1;
-  return rhyme_gpu_sync_to_device(ctx, *handle);
+  // Pin the caller's array for asynchronous copies when asked and possible;
+  // a failure here only costs copy speed.
+  if (pin) {
+    if (cudaHostRegister(cells, (size_t)ncmp * F * sizeof(double), cudaHostRegisterDefault) == cudaSuccess)
+      b->registered_host = true;
+    else
+      cudaGetLastError();
+  }
+  // set up before the upload (the server passes page-locked staging)
+  // reuse a free slot
+  int h = -1;
+  for (int i = 0; i < (int)ctx->boxes.size(); ++i)
+    if (!ctx->boxes[i]) {
+      h = i;
+      break;
+    }
+  if (h < 0) {
+    ctx->boxes.push_back(b);
+    h = (int)ctx->boxes.size() - 1;
+  } else {
+    ctx->boxes[h] = b;
+  }
+  *handle = h;
+  if (!upload) return RHYME_GPU_OK;
+  return rhyme_gpu_sync_to_device(ctx, h);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number, double* cells, const int dims[3],
+                           int ghost, int ncmp, int* handle) {
+  return register_box_impl(ctx, level, number, cells, dims, ghost, ncmp, true, true, handle);
 }
 
 int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
-  cudaStreamSynchronize(ctx->stream);
-  destroy_box(b);
+  destroy_box(b, ctx->stream);
   ctx->boxes[handle] = nullptr;
   return RHYME_GPU_OK;
 }
@@ -374,7 +425,7 @@ int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle) {
     CK(launch_to_f32(b->state[b->cur], b->Uf[b->cur], n, ctx->stream));
     CK(launch_to_f32(b->state[b->cur], b->Uf[1 - b->cur], n, ctx->stream));
   }
-  if (!b->registered_host) return wait_stream(ctx);
+  if (!b->registered_host && !b->host_pinned) return wait_stream(ctx);
   return RHYME_GPU_OK;
 }
 
@@ -768,16 +819,17 @@ struct rhyme_gpu_batch {
 namespace {
 
 void batch_free(rhyme_gpu_batch* B) {
+  cudaStream_t st = B->ctx->stream;
   for (int p = 0; p < 2; ++p) {
     if (B->graph[p]) cudaGraphExecDestroy(B->graph[p]);
     B->graph[p] = nullptr;
-    cudaFree(B->table[p]);
+    if (B->table[p]) cudaFreeAsync(B->table[p], st);
     B->table[p] = nullptr;
   }
-  cudaFree(B->items);
-  cudaFree(B->heads);
-  cudaFree(B->q.e);
-  cudaFree(B->qblock);
+  if (B->items) cudaFreeAsync(B->items, st);
+  if (B->heads) cudaFreeAsync(B->heads, st);
+  if (B->q.e) cudaFreeAsync(B->q.e, st);
+  if (B->qblock) cudaFreeAsync(B->qblock, st);
   B->items = nullptr;
   B->heads = nullptr;
   B->q.e = nullptr;
@@ -883,18 +935,18 @@ int batch_build(rhyme_gpu_batch* B) {
     all.insert(all.end(), lists[k]->begin(), lists[k]->end());
   }
   for (int p = 0; p < 2; ++p) {
-    CK(cudaMalloc(&B->table[p], sizeof(BoxDesc) * std::max(n, 1)));
+    CK(cudaMallocAsync((void**)&B->table[p], sizeof(BoxDesc) * std::max(n, 1), ctx->stream));
     CK(cudaMemcpyAsync(B->table[p], tab[p].data(), sizeof(BoxDesc) * n, cudaMemcpyHostToDevice, ctx->stream));
   }
-  CK(cudaMalloc(&B->items, sizeof(WorkItem) * std::max<size_t>(all.size(), 1)));
+  CK(cudaMallocAsync((void**)&B->items, sizeof(WorkItem) * std::max<size_t>(all.size(), 1), ctx->stream));
   CK(cudaMemcpyAsync(B->items, all.data(), sizeof(WorkItem) * all.size(), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMalloc(&B->heads, 16 * sizeof(int)));
-  CK(cudaMalloc(&B->qblock, 16 * sizeof(int)));
+  CK(cudaMallocAsync((void**)&B->heads, 16 * sizeof(int), ctx->stream));
+  CK(cudaMallocAsync((void**)&B->qblock, 16 * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(B->qblock, 0, 16 * sizeof(int), ctx->stream));
   B->q.cap = 0;
   if (ctx->mixed) {
     B->q.cap = (int)std::min<long long>(std::max<long long>(65536, qcap), 1LL << 30);
-    CK(cudaMalloc(&B->q.e, sizeof(FallbackEntry) * (size_t)B->q.cap));
+    CK(cudaMallocAsync((void**)&B->q.e, sizeof(FallbackEntry) * (size_t)B->q.cap, ctx->stream));
   }
   B->q.n = B->qblock + 0;
   B->q.status = B->qblock + 1;
@@ -913,11 +965,19 @@ int batch_build(rhyme_gpu_batch* B) {
   L.n_update = (int)update.size();
   for (int a = 0; a < 3; ++a) L.n_sweep[a] = (int)sweep[a].size();
   L.heads = B->heads;
-  // one step per parity, captured
+  return RHYME_GPU_OK;
+}
+
+// One step per parity captured in a CUDA graph (on the first run of several
+// steps; short runs, as in a serving loop whose batch changes every few
+// steps, launch directly).
+int batch_capture(rhyme_gpu_batch* B) {
+  rhyme_gpu_ctx* ctx = B->ctx;
   for (int p = 0; p < 2; ++p) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = launch_batch_step(ctx->dp, ctx->mp, ctx->mixed, D, B->table[p], L, B->q, ctx->stream);
+    cudaError_t e = launch_batch_step(ctx->dp, ctx->mp, ctx->mixed, ctx->params.ndim, B->table[p], B->L, B->q,
+                                      ctx->stream);
     cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
     if (e != cudaSuccess || e2 != cudaSuccess) {
       if (e2 == cudaSuccess) cudaGraphDestroy(graph);
@@ -973,8 +1033,16 @@ extern "C" int rhyme_gpu_batch_run(rhyme_gpu_batch* B, int nsteps) {
       break;
     }
   }
+  if (nsteps >= 4 && !B->graph[0]) {
+    int rc = batch_capture(B);
+    if (rc != RHYME_GPU_OK) return rc;
+  }
   for (int s = 0; s < nsteps; ++s) {
-    CK(cudaGraphLaunch(B->graph[B->k], ctx->stream));
+    if (B->graph[0])
+      CK(cudaGraphLaunch(B->graph[B->k], ctx->stream));
+    else
+      CK(launch_batch_step(ctx->dp, ctx->mp, ctx->mixed, ctx->params.ndim, B->table[B->k], B->L, B->q,
+                           ctx->stream));
     B->k ^= 1;
   }
   for (size_t i = 0; i < B->handles.size(); ++i) ctx->boxes[B->handles[i]]->cur = B->base_cur[i] ^ B->k;
@@ -997,3 +1065,288 @@ extern "C" int rhyme_gpu_batch_destroy(rhyme_gpu_batch* B) {
   delete B;
   return RHYME_GPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Serving loop: continuous batching of hydro solves
+// ---------------------------------------------------------------------------
+namespace {
+
+struct ServerReq {
+  rhyme_gpu_request r{};
+  int state = RHYME_GPU_REQ_PENDING;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  int steps_done = 0;
+  int handle = -1;
+  long long bytes = 0;
+  long long cells = 0;
+  void* staging = nullptr;
+  size_t staging_bytes = 0;
+  cudaEvent_t ev = nullptr;
+};
+
+}  // namespace
+
+struct rhyme_gpu_server {
+  rhyme_gpu_ctx* ctx[3] = {nullptr, nullptr, nullptr};
+  long long budget = 0, used = 0;
+  int max_active = 0;
+  int n_active = 0;
+  std::vector<ServerReq> reqs;
+  std::vector<int> pending;  // FIFO (front at index pend_head)
+  size_t pend_head = 0;
+  std::vector<int> active[3];
+  rhyme_gpu_batch* batch[3] = {nullptr, nullptr, nullptr};
+  bool dirty[3] = {false, false, false};
+  std::vector<int> draining;
+  cudaStream_t copy = nullptr;
+  std::chrono::steady_clock::time_point t0;
+  std::vector<std::pair<size_t, void*>> pinned_free;  // page-locked staging pool
+  std::string err;
+  long long cell_updates = 0;
+};
+
+namespace {
+
+double server_now(const rhyme_gpu_server* S) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - S->t0).count();
+}
+
+void* pinned_get(rhyme_gpu_server* S, size_t bytes, size_t* got) {
+  size_t best = (size_t)-1, bi = 0;
+  for (size_t i = 0; i < S->pinned_free.size(); ++i)
+    if (S->pinned_free[i].first >= bytes && S->pinned_free[i].first < best) {
+      best = S->pinned_free[i].first;
+      bi = i;
+    }
+  if (best != (size_t)-1 && best <= 4 * bytes + (1 << 20)) {
+    void* p = S->pinned_free[bi].second;
+    *got = best;
+    S->pinned_free.erase(S->pinned_free.begin() + bi);
+    return p;
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  *got = bytes;
+  return p;
+}
+
+void pinned_put(rhyme_gpu_server* S, void* p, size_t bytes) { S->pinned_free.push_back({bytes, p}); }
+
+int server_fail(rhyme_gpu_server* S, int code, const char* msg) {
+  S->err = msg;
+  return code;
+}
+
+void server_drop_batch(rhyme_gpu_server* S, int k) {
+  if (S->batch[k]) {
+    batch_free(S->batch[k]);
+    delete S->batch[k];
+    S->batch[k] = nullptr;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rhyme_gpu_server_create(const rhyme_gpu_params* base, const double courant[3], long long hbm_budget_bytes,
+                            int max_active, rhyme_gpu_server** out) {
+  if (!base || !courant || !out || hbm_budget_bytes <= 0 || max_active < 1) return RHYME_GPU_EINVAL;
+  *out = nullptr;
+  rhyme_gpu_server* S = new rhyme_gpu_server();
+  S->budget = hbm_budget_bytes;
+  S->max_active = max_active;
+  S->t0 = std::chrono::steady_clock::now();
+  for (int k = 0; k < 3; ++k) {
+    rhyme_gpu_params p = *base;
+    p.ndim = k + 1;
+    p.courant = courant[k];
+    for (int i = 0; i < 6; ++i)
+      if (p.bc[i] < 1 || p.bc[i] > 4) p.bc[i] = RHYME_GPU_OUTFLOW;
+    int rc = rhyme_gpu_create(&S->ctx[k], &p);
+    if (rc != RHYME_GPU_OK) {
+      for (int j = 0; j < k; ++j) rhyme_gpu_destroy(S->ctx[j]);
+      delete S;
+      return rc;
+    }
+  }
+  if (cudaStreamCreateWithFlags(&S->copy, cudaStreamNonBlocking) != cudaSuccess) {
+    for (int k = 0; k < 3; ++k) rhyme_gpu_destroy(S->ctx[k]);
+    delete S;
+    return RHYME_GPU_ECUDA;
+  }
+  *out = S;
+  return RHYME_GPU_OK;
+}
+
+const char* rhyme_gpu_server_last_error(const rhyme_gpu_server* S) { return S ? S->err.c_str() : ""; }
+
+int rhyme_gpu_server_submit(rhyme_gpu_server* S, const rhyme_gpu_request* r, int* id) {
+  if (!S || !r || !id || !r->cells) return RHYME_GPU_EINVAL;
+  if (r->ndim < 1 || r->ndim > 3 || r->nsteps < 0) return server_fail(S, RHYME_GPU_EINVAL, "bad request");
+  for (int a = 0; a < 3; ++a)
+    if ((a < r->ndim && r->dims[a] < 1) || (a >= r->ndim && r->dims[a] != 1))
+      return server_fail(S, RHYME_GPU_EINVAL, "bad request dims");
+  ServerReq q;
+  q.r = *r;
+  q.t_submit = server_now(S);
+  q.bytes = box_device_bytes(r->ndim, S->ctx[0]->mixed, r->dims);
+  q.cells = (long long)r->dims[0] * r->dims[1] * r->dims[2];
+  if (q.bytes > S->budget) return server_fail(S, RHYME_GPU_ENOMEM, "request larger than the HBM budget");
+  S->reqs.push_back(q);
+  *id = (int)S->reqs.size() - 1;
+  S->pending.push_back(*id);
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, int* n_draining) {
+  if (!S) return RHYME_GPU_EINVAL;
+  // 1. finished downloads: copy out of the staging buffer
+  for (size_t i = 0; i < S->draining.size();) {
+    ServerReq& q = S->reqs[S->draining[i]];
+    cudaError_t e = cudaEventQuery(q.ev);
+    if (e == cudaErrorNotReady) {
+      ++i;
+      continue;
+    }
+    if (e != cudaSuccess) return server_fail(S, RHYME_GPU_ECUDA, cudaGetErrorString(e));
+    const int D = q.r.ndim;
+    const Geom g = make_geom(D, q.r.dims);
+    memcpy(q.r.cells, q.staging, (size_t)(D + 2) * g.field * sizeof(double));
+    pinned_put(S, q.staging, q.staging_bytes);
+    q.staging = nullptr;
+    cudaEventDestroy(q.ev);
+    q.ev = nullptr;
+    q.t_done = server_now(S);
+    q.state = RHYME_GPU_REQ_DONE;
+    S->used -= q.bytes;
+    S->draining[i] = S->draining.back();
+    S->draining.pop_back();
+  }
+  // 2. admission, first come first served, against the budget and the cap
+  while (S->pend_head < S->pending.size()) {
+    const int id = S->pending[S->pend_head];
+    ServerReq& q = S->reqs[id];
+    if (S->used + q.bytes > S->budget || S->n_active >= S->max_active) break;
+    const int k = q.r.ndim - 1;
+    rhyme_gpu_ctx* ctx = S->ctx[k];
+    const Geom g = make_geom(q.r.ndim, q.r.dims);
+    const size_t hb = (size_t)(q.r.ndim + 2) * g.field * sizeof(double);
+    q.staging = pinned_get(S, hb, &q.staging_bytes);
+    if (!q.staging) return server_fail(S, RHYME_GPU_ENOMEM, "pinned staging allocation failed");
+    memcpy(q.staging, q.r.cells, hb);
+    int h = -1;
+    int rc = register_box_impl(ctx, 0, id, (double*)q.staging, q.r.dims, 2, q.r.ndim + 2, false, true, &h, true);
+    if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+    rc = rhyme_gpu_set_box_params(ctx, h, q.r.bc, q.r.limiter, q.r.omega);
+    if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+    ctx->boxes[h]->dx = make_dx(q.r.ndim, q.r.dx);
+    q.handle = h;
+    q.state = RHYME_GPU_REQ_ACTIVE;
+    q.t_admit = server_now(S);
+    S->used += q.bytes;
+    S->n_active++;
+    S->active[k].push_back(id);
+    S->dirty[k] = true;
+    S->pend_head++;
+  }
+  // 3. one step of every active request, one batch per dimensionality
+  for (int k = 0; k < 3; ++k) {
+    if (S->active[k].empty()) continue;
+    rhyme_gpu_ctx* ctx = S->ctx[k];
+    if (S->dirty[k] || !S->batch[k]) {
+      server_drop_batch(S, k);
+      std::vector<int> hs;
+      std::vector<double> dxs;
+      for (int id : S->active[k]) {
+        hs.push_back(S->reqs[id].handle);
+        for (int a = 0; a < 3; ++a) dxs.push_back(S->reqs[id].r.dx[a] > 0 ? S->reqs[id].r.dx[a] : 1.0);
+      }
+      int rc = rhyme_gpu_batch_create(ctx, hs.data(), dxs.data(), (int)hs.size(), &S->batch[k]);
+      if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+      S->dirty[k] = false;
+    }
+    int rc = rhyme_gpu_batch_run(S->batch[k], 1);
+    if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+    for (int id : S->active[k]) {
+      S->reqs[id].steps_done++;
+      S->cell_updates += S->reqs[id].cells;
+    }
+  }
+  // 4. retire finished requests: download on the copy stream, free in order
+  for (int k = 0; k < 3; ++k) {
+    rhyme_gpu_ctx* ctx = S->ctx[k];
+    for (size_t i = 0; i < S->active[k].size();) {
+      const int id = S->active[k][i];
+      ServerReq& q = S->reqs[id];
+      if (q.steps_done < q.r.nsteps) {
+        ++i;
+        continue;
+      }
+      Box* b = ctx->boxes[q.handle];
+      cudaEvent_t done_compute;
+      if (cudaEventCreateWithFlags(&done_compute, cudaEventDisableTiming) != cudaSuccess)
+        return server_fail(S, RHYME_GPU_ECUDA, "event");
+      cudaEventRecord(done_compute, ctx->stream);
+      cudaStreamWaitEvent(S->copy, done_compute, 0);
+      cudaEventDestroy(done_compute);
+      cudaMemcpyAsync(q.staging, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, S->copy);
+      cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming);
+      cudaEventRecord(q.ev, S->copy);
+      // the batch tables reference this box: drop the batch before freeing
+      server_drop_batch(S, k);
+      S->dirty[k] = true;
+      destroy_box(b, S->copy);
+      ctx->boxes[q.handle] = nullptr;
+      q.state = RHYME_GPU_REQ_DRAINING;
+      S->draining.push_back(id);
+      S->n_active--;
+      S->active[k][i] = S->active[k].back();
+      S->active[k].pop_back();
+    }
+  }
+  if (n_active) *n_active = S->n_active;
+  if (n_pending) *n_pending = (int)(S->pending.size() - S->pend_head);
+  if (n_draining) *n_draining = (int)S->draining.size();
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_server_request(rhyme_gpu_server* S, int id, int* state, double times[3], int* steps_done) {
+  if (!S || id < 0 || id >= (int)S->reqs.size()) return RHYME_GPU_EINVAL;
+  const ServerReq& q = S->reqs[id];
+  if (state) *state = q.state;
+  if (times) {
+    times[0] = q.t_submit;
+    times[1] = q.t_admit;
+    times[2] = q.t_done;
+  }
+  if (steps_done) *steps_done = q.steps_done;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_server_stats(rhyme_gpu_server* S, long long* cell_updates, long long* hbm_used) {
+  if (!S) return RHYME_GPU_EINVAL;
+  if (cell_updates) *cell_updates = S->cell_updates;
+  if (hbm_used) *hbm_used = S->used;
+  return RHYME_GPU_OK;
+}
+
+int rhyme_gpu_server_destroy(rhyme_gpu_server* S) {
+  if (!S) return RHYME_GPU_OK;
+  for (int k = 0; k < 3; ++k) {
+    if (S->ctx[k]) cudaStreamSynchronize(S->ctx[k]->stream);
+    server_drop_batch(S, k);
+  }
+  if (S->copy) cudaStreamSynchronize(S->copy);
+  for (auto& q : S->reqs) {
+    if (q.ev) cudaEventDestroy(q.ev);
+    if (q.staging) cudaFreeHost(q.staging);
+  }
+  for (auto& f : S->pinned_free) cudaFreeHost(f.second);
+  for (int k = 0; k < 3; ++k) rhyme_gpu_destroy(S->ctx[k]);
+  if (S->copy) cudaStreamDestroy(S->copy);
+  delete S;
+  return RHYME_GPU_OK;
+}
+
+}  // extern "C"

@@ -32,7 +32,18 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
            "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc", "rhyme_gpu_set_box_params",
-           "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy"]
+           "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
+           "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
+           "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
+           "rhyme_gpu_server_destroy"]
+REQ_PENDING, REQ_ACTIVE, REQ_DRAINING, REQ_DONE = 0, 1, 2, 3
+
+
+class Request(C.Structure):
+    """struct rhyme_gpu_request (include/rhyme_gpu.h)."""
+    _fields_ = [("ndim", C.c_int), ("dims", C.c_int * 3), ("nsteps", C.c_int), ("limiter", C.c_int),
+                ("bc", C.c_int * 6), ("omega", C.c_double), ("dx", C.c_double * 3),
+                ("cells", C.POINTER(C.c_double))]
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 
 
@@ -118,6 +129,14 @@ def load():
     L.rhyme_gpu_batch_run.argtypes = [vp, C.c_int]
     L.rhyme_gpu_batch_dt.argtypes = [vp, dp]
     L.rhyme_gpu_batch_destroy.argtypes = [vp]
+    L.rhyme_gpu_server_create.argtypes = [C.POINTER(Params), dp, C.c_longlong, C.c_int, C.POINTER(vp)]
+    L.rhyme_gpu_server_submit.argtypes = [vp, C.POINTER(Request), ip]
+    L.rhyme_gpu_server_tick.argtypes = [vp, ip, ip, ip]
+    L.rhyme_gpu_server_request.argtypes = [vp, C.c_int, ip, dp, ip]
+    L.rhyme_gpu_server_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.rhyme_gpu_server_last_error.argtypes = [vp]
+    L.rhyme_gpu_server_last_error.restype = C.c_char_p
+    L.rhyme_gpu_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -330,3 +349,76 @@ class Context:
         self._check(self.lib.rhyme_gpu_half_step(self.h, _d(u), _d(delta), u.shape[0], int(axis),
                                                  float(dx), float(dt), _d(l), _d(r)))
         return l, r
+
+
+class Server:
+    """rhyme_gpu_server: continuous batching of hydro solves.
+
+    base: gas / Riemann / precision parameters (hydro_params mapping);
+    courant: Courant number per dimensionality (1-D, 2-D, 3-D).
+    """
+
+    def __init__(self, base, courant=(0.8, 0.5, 0.3), hbm_budget=150 << 30, max_active=256):
+        self.lib = load()
+        self._p = params_struct(base)
+        cr = np.asarray(courant, dtype=np.float64)
+        h = C.c_void_p()
+        rc = self.lib.rhyme_gpu_server_create(C.byref(self._p), _d(cr), int(hbm_budget), int(max_active),
+                                              C.byref(h))
+        if rc != OK:
+            raise RhymeGpuError(rc, "rhyme_gpu_server_create failed")
+        self.h = h
+        self._keep = {}
+
+    def _check(self, rc):
+        if rc != OK:
+            raise RhymeGpuError(rc, self.lib.rhyme_gpu_server_last_error(self.h).decode())
+
+    def submit(self, cells, nsteps, dx, limiter, bc, omega=0.0):
+        """Queue one solve; `cells` (NDIM+2, ...) receives the result."""
+        assert cells.dtype == np.float64 and cells.flags.c_contiguous
+        r = Request()
+        nd = cells.ndim - 1
+        r.ndim = nd
+        ext = cells.shape[1:][::-1]
+        for a in range(3):
+            r.dims[a] = ext[a] - 4 if a < nd else 1
+            r.dx[a] = dx[a] if a < len(dx) else 1.0
+        r.nsteps = int(nsteps)
+        r.limiter = int(limiter)
+        for i in range(6):
+            r.bc[i] = int(bc[i]) if i < len(bc) else 2
+        r.omega = float(omega)
+        r.cells = _d(cells)
+        rid = C.c_int()
+        self._check(self.lib.rhyme_gpu_server_submit(self.h, C.byref(r), C.byref(rid)))
+        self._keep[rid.value] = cells
+        return rid.value
+
+    def tick(self):
+        a, p, d = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.rhyme_gpu_server_tick(self.h, C.byref(a), C.byref(p), C.byref(d)))
+        return a.value, p.value, d.value
+
+    def request(self, rid):
+        st = C.c_int()
+        t = np.zeros(3)
+        n = C.c_int()
+        self._check(self.lib.rhyme_gpu_server_request(self.h, int(rid), C.byref(st), _d(t), C.byref(n)))
+        return st.value, t, n.value
+
+    def stats(self):
+        cu, used = C.c_longlong(), C.c_longlong()
+        self._check(self.lib.rhyme_gpu_server_stats(self.h, C.byref(cu), C.byref(used)))
+        return cu.value, used.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rhyme_gpu_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
