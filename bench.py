@@ -1,8 +1,11 @@
 """Benchmark of the GB300 MUSCL-Hancock hydro step (one JSON line on rank 0).
 
-Default workload: 2-D 256x256 periodic shear slab (minmod, courant 0.8,
-gamma 5/3), plain FP64, the configuration the plain GPU path is quoted on.
-A step is one driver iteration (dt -> ghost fill -> solve) over the box.
+Default workload: 3-D 256^3 periodic box with 32 spheres and a harmonic
+density ripple (superbee, courant 0.3, gamma 5/3), in the mixed FP32/FP64
+form, with the plain FP64 path timed on the same box beside it and the
+per-field L1 / Linf difference between the two after 300 steps: the
+configuration the mixed-vs-FP64 metric is quoted on. A step is one driver
+iteration (dt -> ghost fill -> solve) over the box.
 
   value   cell-updates/s with the state resident in HBM, timed with CUDA
           events on the library's stream around each step; L2 is flushed
@@ -10,13 +13,20 @@ A step is one driver iteration (dt -> ghost fill -> solve) over the box.
   e2e     the same metric through the reference-facing C-ABI with the state
           in host memory: per step host->device upload, dt (read back),
           ghost fill, solve and device->host download, wall-clock timed.
-  roofline  HBM roofline of the dominant kernel (the interface-flux pass),
-          from algorithmic bytes per step over its event-timed duration.
+  roofline  HBM roofline of the dominant kernel: the step's algorithmic
+          bytes (U^n read + U^{n+1} written, (NDIM+2) FP64 fields per cell)
+          over that kernel's event-timed duration per step.
   cpu_baseline  the CPU oracle (a restatement of the reference's
           memory-intensive solver with OpenMP over the outer loop) on a
           bounded sample of the same workload, all host threads.
 
---impl reference times that CPU implementation alone on the same config.
+Other workloads (--workload): slab2d (2-D 256^2 shear slab, plain FP64,
+500 steps), riemann1d (1-D 512 cells, 100 steps), spheres3d<N>, batch4096
+(4096 uneven 3-D boxes stepped as one batch; use --steps 10) and serve (a
+seeded Poisson stream of requests served by the continuous-batching server
+against one-at-a-time plain FP64).
+
+--impl reference times the CPU implementation alone on the same config.
 Under torchrun each rank runs an independent replica (the path shards by
 box; a single box is replicated) and value is the sum over ranks.
 """
@@ -36,16 +46,18 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s"
 L2_FLUSH_BYTES = 512 << 20
+DEFAULT_WORKLOAD = "spheres3d256"
 
 
-def workload(name, precision="fp64"):
-    """(cells, dx, params, config dict) of a named workload."""
-    from rhyme_gb300 import ic
+def workload(name, precision=None):
+    """(cells, dx, params, config dict) of a named single-box workload;
+    precision None takes the workload's own."""
+    from rhyme_gb300.params import FP64, MIXED
     cells, dx, p, cfg = _workload(name)
-    if precision == "mixed":
-        from rhyme_gb300.params import MIXED
-        p = dict(p, precision=MIXED)
-        cfg = dict(cfg, workload=cfg["workload"].replace("plain FP64", "mixed FP32/FP64"))
+    prec = precision or cfg["precision"]
+    p = dict(p, precision=MIXED if prec == "mixed" else FP64)
+    form = "mixed FP32/FP64" if prec == "mixed" else "plain FP64"
+    cfg = dict(cfg, workload="%s, %s" % (cfg["workload"], form), precision=prec)
     return cells, dx, p, cfg
 
 
@@ -53,17 +65,18 @@ def _workload(name):
     from rhyme_gb300 import ic
     if name == "slab2d":
         cells, dx, p = ic.slab_2d(n=256, seed=0)
-        cfg = {"workload": "2-D 256x256 periodic shear slab, minmod, courant 0.8, plain FP64",
-               "ndim": 2, "cells": 256 * 256, "steps_in_run": 500}
+        cfg = {"workload": "2-D 256x256 periodic shear slab, minmod, courant 0.8",
+               "ndim": 2, "cells": 256 * 256, "steps_in_run": 500, "precision": "fp64"}
     elif name == "riemann1d":
         cells, dx, p = ic.riemann_1d(n=512, seed=0)
-        cfg = {"workload": "1-D 512-cell seeded Riemann problem, van Leer, courant 0.8, plain FP64",
-               "ndim": 1, "cells": 512, "steps_in_run": 100}
+        cfg = {"workload": "1-D 512-cell seeded Riemann problem, van Leer, courant 0.8",
+               "ndim": 1, "cells": 512, "steps_in_run": 100, "precision": "fp64"}
     elif name.startswith("spheres3d"):
         n = int(name[len("spheres3d"):] or 256)
         cells, dx, p = ic.spheres_3d(n=n, seed=0)
-        cfg = {"workload": "3-D %d^3 periodic, 32 spheres + harmonic density, superbee, courant %.2g, plain FP64"
-                           % (n, p["courant"]), "ndim": 3, "cells": n ** 3, "steps_in_run": 300}
+        cfg = {"workload": "3-D %d^3 periodic, 32 spheres + harmonic density, superbee, courant %.2g"
+                           % (n, p["courant"]), "ndim": 3, "cells": n ** 3, "steps_in_run": 300,
+               "precision": "mixed"}
     else:
         raise SystemExit("unknown workload %s" % name)
     return cells, dx, p, cfg
@@ -72,6 +85,10 @@ def _workload(name):
 def algorithmic_bytes_per_cell(ndim):
     # U^n read once + U^{n+1} written once, NDIM+2 FP64 fields
     return 2 * (ndim + 2) * 8
+
+
+def dtype_name(prec):
+    return "f64" if prec == "fp64" else "f32+f64"
 
 
 class ClockSampler:
@@ -85,7 +102,6 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
-        self.t0 = None
 
     def start(self):
         try:
@@ -103,18 +119,10 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.rows.append((time.time(), line.strip()))
 
-    def mark(self):
-        return time.time()
-
-    def stop(self, t_begin, t_end):
+    def summary(self, t_begin, t_end):
+        """Median SM clock and active throttle reasons between two times."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
         rows = [r for t, r in self.rows if t_begin - 0.15 <= t <= t_end + 0.15] or [r for _, r in self.rows[-3:]]
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -132,6 +140,16 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+    def stop(self):
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
 
 
 def measured_peaks():
@@ -162,10 +180,12 @@ def cpu_sample(cells, dx, p, steps_cap, budget_s, nthreads):
     import oracle
     c = cells.copy()
     interior = int(np.prod([s - 4 for s in c.shape[1:]]))
+    t0 = time.perf_counter()
     oracle.run(p, c, dx, 1, nthreads=nthreads)  # warm (allocates the workspace)
+    first = time.perf_counter() - t0
     done, t = 0, 0.0
     chunk = 1
-    while done < steps_cap and t < budget_s:
+    while done < steps_cap and t + first < budget_s:
         t0 = time.perf_counter()
         oracle.run(p, c, dx, chunk, nthreads=nthreads)
         t += time.perf_counter() - t0
@@ -173,6 +193,8 @@ def cpu_sample(cells, dx, p, steps_cap, budget_s, nthreads):
         chunk = min(chunk * 2, steps_cap - done) if done < steps_cap else 0
         if chunk <= 0:
             break
+    if done == 0:  # a single step is already beyond the budget
+        return interior / first, 1, first
     return interior * done / t, done, t
 
 
@@ -182,8 +204,7 @@ def dist_init():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl")
     return rank, local, world
 
 
@@ -194,68 +215,70 @@ def barrier(world):
 
 
 def allmax(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from rhyme_gb300.shard import reduce_scalar
+    return reduce_scalar(x, world, "max", device="cuda")
+
+
+def allsum(x, world):
+    from rhyme_gb300.shard import reduce_scalar
+    return reduce_scalar(x, world, "sum", device="cuda")
+
+
+def launches_per_step(prec, ndim):
+    """Kernels of this library launched per single-box step: FP64 cfl, ghost
+    fill, faces, fluxes, update; mixed cfl, ghost fill (FP64 and FP32), one
+    sweep per axis, FP64 fix-up and FP32 refresh of the queued interfaces."""
+    return 5 if prec == "fp64" else 5 + ndim
+
+
+def reference_sample(name, cells, dx, p, cfg):
+    """The bounded sample one reference-arm step runs: the whole box, or for
+    3-D boxes of 128^3 and more its first 16 z-planes (with the box's own
+    periodic boundaries), so that a step takes well under a second."""
+    if cfg["ndim"] == 3 and cells.shape[1] - 4 >= 128:
+        nz = 16
+        sub = np.ascontiguousarray(cells[:, :nz + 4])
+        n = int(np.prod([s - 4 for s in sub.shape[1:]]))
+        return sub, n, "first %d z-planes of the %s box (%d cells) per step" % (
+            nz, "x".join(str(s - 4) for s in cells.shape[1:][::-1]), n)
+    return cells.copy(), cfg["cells"], "the whole box per step"
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    cells, dx, p, cfg = workload(args.workload)
-    p = dict(p, precision=0)  # the CPU implementation is FP64
+    from rhyme_gb300.params import FP64
+    if args.workload in ("batch4096", "serve"):
+        raise SystemExit("--impl reference covers the single-box workloads")
+    cells, dx, p, cfg = workload(args.workload, "fp64")
+    p = dict(p, precision=FP64)  # the CPU implementation is FP64
     import oracle
     nthreads = os.cpu_count() or 1
-    interior = cfg["cells"]
-    c = cells.copy()
+    c, n, what = reference_sample(args.workload, cells, dx, p, cfg)
     if args.warmup:
         oracle.run(p, c, dx, args.warmup, nthreads=nthreads)
     t0 = time.perf_counter()
     oracle.run(p, c, dx, args.steps, nthreads=nthreads)
     t = time.perf_counter() - t0
-    v = interior * args.steps / t
-    sample = "%d timed steps of the workload after %d warm-up steps, OpenMP over the outer cell loop" % (
-        args.steps, args.warmup)
+    v = n * args.steps / t
+    sample = "%d timed steps after %d warm-up steps; %s; OpenMP over the outer cell loop" % (
+        args.steps, args.warmup, what)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": cfg,
+            "data": "synthetic", "config": dict(cfg, workload=cfg["workload"].replace("mixed FP32/FP64", "plain FP64")),
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args, rank, local, world):
+def time_steps(ctx, box, dx, K, flush, stream):
+    """K single steps, each bracketed by CUDA events on the library's stream,
+    with an L2 flush between them outside the events; ms per step."""
     import torch
-    from rhyme_gb300 import gpu
-    torch.cuda.set_device(local)
-    cells, dx, p, cfg = workload(args.workload, args.precision)
-    ndim = p["ndim"]
-    interior = cfg["cells"]
-    K, W = args.steps, args.warmup
-
-    ctx = gpu.Context(p)
-    state = cells.copy()
-    box = ctx.register_box(state)
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    ctx.run(box, dx, W, trace=False)
-    ctx.synchronize()
-
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    barrier(world)
-    torch.cuda.synchronize()
-    ctx.synchronize()
-    t_begin = time.time()
     for k in range(K):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -264,12 +287,78 @@ def run_gpu(args, rank, local, world):
         ends[k].record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def run_gpu(args, rank, local, world):
+    import torch
+    from rhyme_gb300 import gpu
+    from rhyme_gb300.metrics import field_errors
+    from rhyme_gb300.params import FP64
+    torch.cuda.set_device(local)
+    cells, dx, p, cfg = workload(args.workload, args.precision)
+    prec = cfg["precision"]
+    ndim = p["ndim"]
+    interior = cfg["cells"]
+    K, W = args.steps, args.warmup
+    compare = prec == "mixed" and not args.no_compare
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+
+    # headline form
+    ctx = gpu.Context(p)
+    state = cells.copy()
+    box = ctx.register_box(state)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.run(box, dx, W, trace=False)
+    ctx.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    t_begin = time.time()
+    per_step = time_steps(ctx, box, dx, K, flush, stream)
     barrier(world)
     t_end = time.time()
-    clk = clocks.stop(t_begin, t_end)
-    per_step = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    clk = clocks.summary(t_begin, t_end)
     ms = allmax(sum(per_step), world)
     value = world * interior * K / (ms * 1e-3)
+
+    # plain FP64 on the same box, and the difference after the run's steps
+    cmp = None
+    if compare:
+        pc = dict(p, precision=FP64)
+        ctx_c = gpu.Context(pc)
+        state_c = cells.copy()
+        box_c = ctx_c.register_box(state_c)
+        stream_c = torch.cuda.ExternalStream(ctx_c.stream)
+        ctx_c.run(box_c, dx, W, trace=False)
+        ctx_c.synchronize()
+        barrier(world)
+        tc0 = time.time()
+        per_c = time_steps(ctx_c, box_c, dx, K, flush, stream_c)
+        barrier(world)
+        tc1 = time.time()
+        ms_c = allmax(sum(per_c), world)
+        value_c = world * interior * K / (ms_c * 1e-3)
+        n_acc = max(cfg["steps_in_run"], W + K)
+        for c_, b_ in ((ctx, box), (ctx_c, box_c)):
+            if n_acc > W + K:
+                c_.run(b_, dx, n_acc - (W + K), trace=False)
+            c_.sync_to_host(b_)
+        fb = ctx.fallback_count(box)
+        errs = field_errors(state, state_c, ndim)
+        names = ["rho"] + ["rho_v%s" % "xyz"[a] for a in range(ndim)] + ["e_tot"]
+        cmp = {"fp64_value": value_c, "fp64_ms_per_step": ms_c / K, "mixed_over_fp64": value / value_c,
+               "fp64_clocks": clocks.summary(tc0, tc1),
+               "errors_vs_fp64": {"after_steps": n_acc, "definition": "relative L1 = sum|d|/sum|f64|, "
+                                  "relative Linf = max|d|/max|f64| over the interior",
+                                  "l1": dict(zip(names, [e[0] for e in errs])),
+                                  "linf": dict(zip(names, [e[1] for e in errs]))},
+               "fp64_interfaces_redone_in_run": fb}
+        ctx_c.close()
+        # the headline box continues from its own state for the profile below
+    clocks.stop()
 
     # phase timing of the same step (direct launches, events between kernels)
     phases = ctx.profile_steps(box, dx, max(5, min(50, K)))
@@ -277,7 +366,8 @@ def run_gpu(args, rank, local, world):
     bpc = algorithmic_bytes_per_cell(ndim)
     peak, peak_kind = measured_peaks()
     achieved = interior * bpc / (phases[dom] * 1e-3) / 1e9
-    traffic = ncu_traffic(args.workload, dom)
+    traffic = ncu_traffic("%s-%s" % (args.workload, prec), dom)
+    ctx.close()
 
     # end to end through the C-ABI with the state in host memory
     host = cells.copy()
@@ -285,37 +375,37 @@ def run_gpu(args, rank, local, world):
     b2 = ctx2.register_box(host)
     hydro_bytes = (ndim + 2) * int(np.prod(host.shape[1:])) * 8
     ke = max(1, min(K, args.e2e_steps))
-    for _ in range(min(W, 3)):
+
+    def e2e_step():
         ctx2.sync_to_device(b2)
         dt = ctx2.cfl_time_step(b2, dx)
         ctx2.set_boundaries(b2)
         ctx2.muscl_hancock_solve(b2, dx, dt)
         ctx2.sync_to_host(b2)
+
+    for _ in range(min(W, 3)):
+        e2e_step()
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(ke):
-        ctx2.sync_to_device(b2)
-        dt = ctx2.cfl_time_step(b2, dx)
-        ctx2.set_boundaries(b2)
-        ctx2.muscl_hancock_solve(b2, dx, dt)
-        ctx2.sync_to_host(b2)
+        e2e_step()
     te = allmax(time.perf_counter() - t0, world)
     barrier(world)
     e2e = world * interior * ke / te
+    ctx2.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
-        v, n, t = cpu_sample(cells, dx, p, cfg["steps_in_run"], args.cpu_budget, nthreads)
+        v, n, t = cpu_sample(cells, dx, dict(p, precision=FP64), cfg["steps_in_run"], args.cpu_budget, nthreads)
         cpu = {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
-               "sample": "first %d steps of the same workload (%.1f s), CPU oracle, OpenMP" % (n, t)}
+               "sample": "first %d steps of the same workload (%.1f s), CPU oracle (FP64), OpenMP" % (n, t)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "ms_per_step_median": statistics.median(per_step),
                 "ms_per_step_max": max(per_step), "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-                "data": "synthetic",
+                "vs_baseline": None, "dtype": dtype_name(prec), "data": "synthetic",
                 "config": dict(cfg, l2="flushed (512 MiB write) between timed steps, outside the events",
                                parallelism="replicas" if world > 1 else "single box"),
                 "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": hydro_bytes + 8,
@@ -323,32 +413,178 @@ def run_gpu(args, rank, local, world):
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": traffic, "bytes_per_cell_update": bpc,
-                             "note": "the plain FP64 path is bound by the FP64 pipe, not HBM"},
+                             "step_achieved": value / world * bpc / 1e9,
+                             "note": "compute-bound: FP64 pipe (plain) / FP32 pipe and SFU (mixed), not HBM"},
                 "phases_ms": phases, "clocks": clk,
-                "gpu_launches": (5 if args.precision == "fp64" else 3 + ndim) * K,
+                "gpu_launches": launches_per_step(prec, ndim) * K,
                 "cpu_baseline": cpu}
+        if cmp is not None:
+            line["vs_fp64"] = cmp
         print(json.dumps(line), flush=True)
-    ctx2.close()
-    ctx.close()
+
+
+def run_batch(args, rank, local, world):
+    """4096 uneven 3-D boxes (edges from {8..64} per axis, Riemann or sphere
+    ICs, reflective/outflow faces, van Albada) stepped as one batch: a
+    work-queue launch per pass, the step captured in a CUDA graph, each box
+    with its own dt. Mixed form headline, plain FP64 beside it, errors of
+    mixed against FP64 after the run. Ranks take cost-balanced shares of the
+    boxes (rhyme_gb300.shard)."""
+    import torch
+    from rhyme_gb300 import gpu, ic
+    from rhyme_gb300.params import FP64, MIXED
+    torch.cuda.set_device(local)
+    from rhyme_gb300 import shard
+    items = ic.batch_boxes(args.nboxes, seed=0)
+    items = shard.my_share(items, [shard.box_cost(c) for c, _, _ in items], rank, world)
+    interior = sum(int(np.prod([s - 4 for s in c.shape[1:]])) for c, _, _ in items)
+    K, W = args.steps, args.warmup
+    prec = args.precision or "mixed"
+    order = [prec] + ([] if args.no_compare else ["fp64" if prec == "mixed" else "mixed"])
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    res, finals = {}, {}
+    for pr in order:
+        base = dict(items[0][2], precision=MIXED if pr == "mixed" else FP64)
+        states = [c.copy() for c, _, _ in items]
+        ctx = gpu.Context(base)
+        boxes = []
+        for st, (_, dx, p) in zip(states, items):
+            b = ctx.register_box(st)
+            ctx.set_box_params(b, bc=p["bc"], limiter=p["limiter"], omega=p["omega"])
+            boxes.append(b)
+        bt = ctx.batch(boxes, [dx for _, dx, _ in items])
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        bt.run(W)
+        ctx.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        t_begin = time.time()
+        ev0.record(stream)
+        bt.run(K)
+        ev1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        barrier(world)
+        t_end = time.time()
+        ms = allmax(ev0.elapsed_time(ev1), world)
+        res[pr] = {"value": allsum(interior, world) * K / (ms * 1e-3), "ms_per_step": ms / K,
+                   "clocks": clocks.summary(t_begin, t_end)}
+        for b in boxes:
+            ctx.sync_to_host(b)
+        bt.close()
+        ctx.close()
+        finals[pr] = states
+    clocks.stop()
+    cmp = None
+    if len(order) == 2:
+        a, b = finals["mixed"], finals["fp64"]
+        d1 = np.zeros(5)
+        s1 = np.zeros(5)
+        dm = np.zeros(5)
+        sm = np.zeros(5)
+        bad64, bad_mixed_only, used = 0, 0, 0
+        for x, y in zip(a, b):
+            xi, yi = x[:, 2:-2, 2:-2, 2:-2], y[:, 2:-2, 2:-2, 2:-2]
+            ok64 = bool(np.isfinite(yi).all() and yi[0].min() > 0)
+            okm = bool(np.isfinite(xi).all() and xi[0].min() > 0)
+            if not ok64:
+                bad64 += 1
+                continue
+            if not okm:
+                bad_mixed_only += 1
+                continue
+            used += 1
+            d = np.abs(xi - yi).reshape(5, -1)
+            r = np.abs(yi).reshape(5, -1)
+            d1 += d.sum(1)
+            s1 += r.sum(1)
+            dm = np.maximum(dm, d.max(1))
+            sm = np.maximum(sm, r.max(1))
+        names = ["rho", "rho_vx", "rho_vy", "rho_vz", "e_tot"]
+        cmp = {"after_steps": W + K, "definition": "relative L1 = sum|d|/sum|f64|, relative Linf = "
+               "max|d|/max|f64| over the interiors of the boxes that stay finite with positive density "
+               "in FP64", "boxes_compared": used,
+               "boxes_failing_in_fp64": bad64, "boxes_failing_in_mixed_only": bad_mixed_only,
+               "l1": dict(zip(names, (d1 / s1).tolist())), "linf": dict(zip(names, (dm / sm).tolist()))}
+    if rank == 0:
+        h = res[prec]
+        line = {"metric": METRIC, "value": h["value"], "unit": METRIC, "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": dtype_name(prec), "data": "synthetic",
+                "config": {"workload": "%d uneven 3-D boxes (edges 8..64 per axis), Riemann or sphere ICs, "
+                                       "van Albada, courant 0.3, one batch, %s" % (args.nboxes, prec),
+                           "cells": interior, "boxes": len(items),
+                           "l2": "inputs larger than L2 (%.1f GB of FP64 state)" % (interior * 40 / 1e9),
+                           "parallelism": "boxes sharded over ranks" if world > 1 else "one batch"},
+                "e2e": None, "clocks": h["clocks"],
+                "gpu_launches": launches_per_step(prec, 3) * K, "forms": res, "mixed_vs_fp64": cmp}
+        if "fp64" in res and "mixed" in res:
+            line["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, rank, local, world):
+    """A seeded Poisson stream of requests served by the continuous-batching
+    server (mixed precision, max 256 active, 150 GB budget) and the same
+    stream served one request at a time in plain FP64; p50/p99 latency
+    (submission to result in host memory) and cell-updates/s over the
+    makespan of each."""
+    import torch
+    from rhyme_gb300 import serving
+    from rhyme_gb300.params import FP64, MIXED, hydro_params
+    torch.cuda.set_device(local)
+    stream = serving.make_stream(n=args.requests, rate=args.rate, seed=rank)
+    out = {}
+    for name, prec, cap in (("continuous_mixed", MIXED, 256), ("one_at_a_time_fp64", FP64, 1)):
+        r = serving.replay(stream, hydro_params(3, precision=prec), hbm_budget=150 << 30, max_active=cap)
+        lat = r["latencies"]
+        out[name] = {"value": r["cell_updates"] / r["makespan"], "p50_s": float(np.percentile(lat, 50)),
+                     "p99_s": float(np.percentile(lat, 99)), "makespan_s": r["makespan"],
+                     "cell_updates": r["cell_updates"], "peak_active": r["peak_active"]}
+    h = out["continuous_mixed"]
+    value = allsum(h["value"], world)
+    if rank == 0:
+        cu = sum(int(np.prod([s - 4 for s in q["cells"].shape[1:]])) * q["nsteps"] for q in stream)
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.requests,
+                "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": "Poisson stream, %d requests at %.3g/s, seed 0; 1-/2-/3-D equiprobable, "
+                                       "cells log-uniform in [256, 128^3], 50-500 steps; 150 GB budget"
+                                       % (args.requests, args.rate), "cell_updates": cu},
+                "latency_s": {"p50": h["p50_s"], "p99": h["p99_s"]},
+                "e2e": {"value": value, "unit": METRIC, "note": "host arrays in, results drained to host"},
+                "forms": out,
+                "throughput_over_one_at_a_time": h["value"] / out["one_at_a_time_fp64"]["value"]}
+        print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="slab2d")
-    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the other precision")
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--nboxes", type=int, default=4096)
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--rate", type=float, default=8.0)
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and args.workload != "serve":
         raise SystemExit("at least 3 warm-up steps")
     rank, local, world = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batch4096":
+        run_batch(args, rank, local, world)
+    elif args.workload == "serve":
+        run_serve(args, rank, local, world)
     else:
         run_gpu(args, rank, local, world)
     if world > 1:

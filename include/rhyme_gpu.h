@@ -60,6 +60,16 @@ enum { RHYME_GPU_CPU_INTENSIVE = 1, RHYME_GPU_MEMORY_INTENSIVE = 2 };
 enum { RHYME_GPU_FP64 = 0, RHYME_GPU_MIXED = 1 };
 
 /*
+ * Tile shapes of the mixed-precision sweeps (no reference counterpart):
+ * TUNE_AUTO times the candidate shapes (cells along the sweep axis x
+ * pencils: 8x32, 16x16, 32x8, 64x4; 64..512 cells in 1-D) on the first box
+ * of each box-size class a context meets and keeps the fastest per class;
+ * TUNE_FIXED uses a size rule without timing launches. Results do not
+ * depend on the shape. Ignored in FP64 mode.
+ */
+enum { RHYME_GPU_TUNE_AUTO = 0, RHYME_GPU_TUNE_FIXED = 1 };
+
+/*
  * Run parameters: the values Rhyme's modules hold after load_params
  * (rhyme_param_parser_load_params.f90: BCs :259-293, courant :307, gas :314,
  * Riemann :493-499, limiter :512-513, solver :523) and rhyme_*_init.
@@ -71,7 +81,7 @@ typedef struct rhyme_gpu_params {
   int solver_type;   /* mh%solver_type */
   int bc[6];         /* bc%types(left, right, bottom, top, back, front) */
   int precision;     /* RHYME_GPU_FP64 or RHYME_GPU_MIXED */
-  int reserved;      /* must be 0 */
+  int sweep_tuning;  /* RHYME_GPU_TUNE_AUTO (0) or RHYME_GPU_TUNE_FIXED (1) */
   double gamma;      /* get_gamma(), rhyme_thermo_base_get_gamma.f90:8-19 */
   double kb_amu;     /* units%kb%v / units%amu%v, rhyme_thermo_base.f90:130 */
   double courant;    /* cfl%courant_number */
@@ -179,8 +189,10 @@ int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  * Instrumentation (no reference counterpart): runs nsteps driver steps with
  * direct launches and CUDA events between the library's kernels on the
  * context stream; ms[5] receives the mean milliseconds per launch of the
- * phases cfl, ghost_fill, faces, fluxes, update. The state advances nsteps
- * steps exactly as rhyme_gpu_run would advance it.
+ * phases cfl, ghost_fill, faces, fluxes, update (RHYME_GPU_FP64) or cfl,
+ * ghost_fill, sweep_x, sweep_y, sweep_z (RHYME_GPU_MIXED; the last one that
+ * runs includes the FP64 fix-up, absent axes read 0). The state advances
+ * nsteps steps exactly as rhyme_gpu_run would advance it.
  */
 int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
                             int nsteps, double ms[5]);
@@ -191,6 +203,16 @@ int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  * since the last query (0 in FP64 mode); clears the counter.
  */
 int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count);
+
+/*
+ * Instrumentation (no reference counterpart): the tile shape of each axis of
+ * the box's mixed-precision sweeps (cells along the axis, pencils), as the
+ * autotuner or the size rule chose it; tunes the box's size classes first
+ * if needed (dx: cell size used for the timing launches). Zeros for absent
+ * axes and in FP64 mode.
+ */
+int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int tile_cells[3],
+                         int tile_pencils[3]);
 
 /*
  * No counterpart in the reference: one plain-FP64 MUSCL-Hancock update

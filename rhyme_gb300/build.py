@@ -21,15 +21,21 @@ LIB = os.path.join(OUT_DIR, "librhyme_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # translation unit -> extra nvcc flags
-UNITS = {
-    "kernels_box.cu": ["--fmad=false"],
-    "kernels_elem.cu": ["--fmad=false"],
-    "rhyme_gpu.cu": ["--fmad=false"],
-    "kernels_mixed.cu": [],
-    "noalloc.cu": ["--fmad=false"],
-    "kernels_batch.cu": ["--fmad=false"],
-}
-HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "box_elems.cuh"]
+# (object name, source, extra flags). The plain FP64 units are compiled
+# without FMA contraction (--fmad=false) so that their arithmetic matches the
+# CPU oracle operation for operation; the mixed-precision units keep it.
+UNITS = [
+    ("kernels_box", "kernels_box.cu", ["--fmad=false"]),
+    ("kernels_elem", "kernels_elem.cu", ["--fmad=false"]),
+    ("rhyme_gpu", "rhyme_gpu.cu", ["--fmad=false"]),
+    ("kernels_mixed", "kernels_mixed.cu", []),
+    ("sweeps_1d", "sweeps.cu", ["-DSWEEP_D=1"]),
+    ("sweeps_2d", "sweeps.cu", ["-DSWEEP_D=2"]),
+    ("sweeps_3d", "sweeps.cu", ["-DSWEEP_D=3"]),
+    ("noalloc", "noalloc.cu", ["--fmad=false"]),
+    ("kernels_batch", "kernels_batch.cu", ["--fmad=false"]),
+]
+HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "box_elems.cuh", "sweep.cuh"]
 
 
 def nvcc():
@@ -40,7 +46,7 @@ def nvcc():
 
 
 def _deps():
-    deps = [os.path.join(CSRC, u) for u in UNITS] + [os.path.join(CSRC, h) for h in HEADERS]
+    deps = sorted({os.path.join(CSRC, src) for _, src, _ in UNITS}) + [os.path.join(CSRC, h) for h in HEADERS]
     deps.append(os.path.join(ROOT, "include", "rhyme_gpu.h"))
     deps.append(os.path.abspath(__file__))
     return deps
@@ -53,9 +59,9 @@ def needs_build():
     return any(os.path.getmtime(p) > t for p in _deps() if os.path.exists(p))
 
 
-def _compile(unit, flags, verbose):
+def _compile(name, unit, flags, verbose):
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(OUT_DIR, unit + ".o")
+    obj = os.path.join(OUT_DIR, name + ".o")
     cmd = [nvcc()] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                              "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj] + flags
     if verbose:
@@ -72,7 +78,7 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
+        objs = list(ex.map(lambda u: _compile(u[0], u[1], u[2], verbose), UNITS))
     tmp = LIB + ".tmp.%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
     if verbose:

@@ -173,8 +173,7 @@ __global__ void __launch_bounds__(256)
 template <int D>
 cudaError_t batch_step_d(const DevParams& P, const MixedParams& M, bool mixed, const BoxDesc* TB,
                          const BatchLists& L, FallbackQueue q, cudaStream_t st) {
-  // queue heads: 0 cfl, 1 ghost, 2 faces, 3 flux, 4 update, 5..7 sweeps, 8 ghost f32
-  cudaError_t e = cudaMemsetAsync(L.heads, 0, 16 * sizeof(int), st);
+  cudaError_t e = cudaMemsetAsync(L.heads, 0, kBatchHeads * sizeof(int), st);
   if (e != cudaSuccess) return e;
   if (mixed) {
     e = launch_batch_cfl_mixed(M, P.courant, TB, L, st);
@@ -184,7 +183,7 @@ cudaError_t batch_step_d(const DevParams& P, const MixedParams& M, bool mixed, c
   }
   if (L.n_ghost) {
     batch_ghost_kernel<D, double><<<152 * 4, 256, 0, st>>>(TB, L.ghost, L.n_ghost, L.heads + 1, false);
-    if (mixed) batch_ghost_kernel<D, float><<<152 * 4, 256, 0, st>>>(TB, L.ghost, L.n_ghost, L.heads + 8, true);
+    if (mixed) batch_ghost_kernel<D, float><<<152 * 4, 256, 0, st>>>(TB, L.ghost, L.n_ghost, L.heads + kHeadGhostF32, true);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

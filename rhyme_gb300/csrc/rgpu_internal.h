@@ -31,19 +31,19 @@ struct MixedParams {
   int ndim;
   int limiter;
   float omega;
+  double omega64;
 };
 
-// One interface queued for the FP64 Riemann solver by a mixed sweep: its
-// axis, the index along that axis of its left cell (0..N), the offset of the
-// left cell and the FP32 face states on either side.
+// One interface queued for the FP64 solver by a mixed sweep: its axis, the
+// index along that axis of its left cell (0..N) and the offset of that cell.
+// The fix-up redoes the whole interface (slopes, half step, Riemann problem)
+// in FP64 from the FP64 state at the start of the step.
 struct FallbackEntry {
   int axis;
   int ga;
   int box;  // index in the batch's box table (0 for a single box)
   int pad;
   long long o;
-  float l[5];
-  float r[5];
 };
 
 struct FallbackQueue {
@@ -52,6 +52,37 @@ struct FallbackQueue {
   int cap;
   int* status;  // bit 1: queue overflow
   int* total;   // running count of FP64 interfaces (statistics)
+};
+
+// Tile shapes of the mixed sweeps, the autotuner's candidate set: S cells
+// along the sweep axis x P pencils, S * P = 256 for 2-/3-D boxes; 1-D boxes
+// have a single pencil.
+constexpr int kSweepShapes = 4;
+
+__host__ __device__ inline void sweep_shape(int ndim, int shape, int* S, int* P) {
+  if (ndim == 1) {
+    *S = 64 << shape;  // 64, 128, 256, 512
+    *P = 1;
+  } else {
+    *S = 8 << shape;  // 8x32, 16x16, 32x8, 64x4
+    *P = 256 / *S;
+  }
+}
+
+// Shape used without tuning: the smallest S that covers the box along the
+// axis, up to 32 along x (pencils stay 8 cells wide) and 16 along y and z
+// (pencils along x stay 16 cells wide, for coalescing); 256 cells in 1-D.
+inline int default_sweep_shape(int ndim, int axis, int nA) {
+  if (ndim == 1) return 2;
+  const int cap = (axis == 0) ? 2 : 1;
+  int k = 0;
+  while (k < cap && (8 << k) < nA) ++k;
+  return k;
+}
+
+// Tile shape per axis of one box's mixed sweeps.
+struct SweepPlan {
+  int shape[3];
 };
 
 // Geometry of one box in the reference layout: component blocks of
@@ -120,7 +151,7 @@ cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& 
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
                                   double* Unew, float* Ufnew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
-                                  cudaStream_t st);
+                                  const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 
 // ---- batches of boxes (kernels_batch.cu) ---------------------------------
@@ -160,12 +191,53 @@ struct BatchLists {
   const WorkItem* faces;
   const WorkItem* flux;
   const WorkItem* update;
-  const WorkItem* sweep[3];
-  int n_cfl, n_ghost, n_faces, n_flux, n_update, n_sweep[3];
-  int* heads;  // one queue head per pass (reset before each step)
+  const WorkItem* sweep[3][kSweepShapes];  // tiles of each axis, grouped by shape
+  int n_cfl, n_ghost, n_faces, n_flux, n_update, n_sweep[3][kSweepShapes];
+  int* heads;  // one queue head per pass (kBatchHeads, reset before each step)
 };
 
-void sweep_tiles(int ndim, int axis, const int* n, int* tS, int* tP);
+// Tile count of a sweep of a box of dims n along `axis` with tile shape
+// `shape` (the work items of a batch enumerate these).
+long long sweep_tile_count(int ndim, int axis, int shape, const int* n);
+
+// One mixed sweep of a box along `axis` with tile shape `shape`
+// (sweeps.cu, compiled once per dimensionality).
+#define RGPU_SWEEP_DECL(D)                                                                              \
+  cudaError_t launch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const float* Uf,         \
+                                    const double* U, const Geom& g, const Dx& dx, const double* dtp,    \
+                                    float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,     \
+                                    cudaStream_t st);                                                   \
+  cudaError_t launch_batch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const BoxDesc* TB, \
+                                          const WorkItem* items, int n, int* head, const FallbackQueue& q, \
+                                          cudaStream_t st);
+RGPU_SWEEP_DECL(1)
+RGPU_SWEEP_DECL(2)
+RGPU_SWEEP_DECL(3)
+#undef RGPU_SWEEP_DECL
+
+inline cudaError_t launch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
+                                     const double* U, const Geom& g, const Dx& dx, const double* dtp,
+                                     float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,
+                                     cudaStream_t st) {
+  switch (ndim) {
+    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+inline cudaError_t launch_batch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M,
+                                           const BoxDesc* TB, const WorkItem* items, int n, int* head,
+                                           const FallbackQueue& q, cudaStream_t st) {
+  switch (ndim) {
+    case 1: return launch_batch_sweep_axis_1(axis, shape, M, TB, items, n, head, q, st);
+    case 2: return launch_batch_sweep_axis_2(axis, shape, M, TB, items, n, head, q, st);
+    case 3: return launch_batch_sweep_axis_3(axis, shape, M, TB, items, n, head, q, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_batch_cfl_mixed(const MixedParams& M, double courant, const BoxDesc* TB,
                                    const BatchLists& L, cudaStream_t st);
 cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const BatchLists& L,
@@ -173,6 +245,12 @@ cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const B
 cudaError_t launch_batch_step(const DevParams& P, const MixedParams& M, bool mixed, int ndim,
                               const BoxDesc* table, const BatchLists& L, FallbackQueue q,
                               cudaStream_t st);
+
+// Queue heads of a batch step: 0 cfl, 1 ghost, 2 faces, 3 flux, 4 update,
+// 5 ghost (FP32 mirror), 6 + 4 * axis + shape the sweeps.
+constexpr int kBatchHeads = 32;
+constexpr int kHeadGhostF32 = 5;
+constexpr int kHeadSweep0 = 6;
 
 // Chunk sizes of the batched passes (elements per work item).
 constexpr int kBatchChunk = 256;

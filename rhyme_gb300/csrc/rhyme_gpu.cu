@@ -14,6 +14,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <map>
 #include <vector>
 
 #include "../../include/rhyme_gpu.h"
@@ -47,6 +48,8 @@ struct Box {
   DevParams dp{};   // the context's parameters with this box's overrides
   MixedParams mp{};
   Dx dx{};          // cell size for batched steps (rhyme_gpu_batch_create)
+  SweepPlan plan{};  // tile shape per axis of the mixed sweeps
+  bool plan_valid = false;
 };
 
 }  // namespace
@@ -64,6 +67,7 @@ struct rhyme_gpu_ctx {
   void* elem_buf = nullptr;      // growable device buffer for element calls
   size_t elem_cap = 0;
   double timeout_s = 600.0;
+  std::map<int, int> tuned;  // box-size class -> tile shape (mixed sweeps)
 };
 
 namespace {
@@ -131,6 +135,8 @@ int validate(rhyme_gpu_ctx* ctx, const rhyme_gpu_params* p) {
     return fail(ctx, RHYME_GPU_EINVAL, "Unknown solver type %d", p->solver_type);
   if (p->precision != RHYME_GPU_FP64 && p->precision != RHYME_GPU_MIXED)
     return fail(ctx, RHYME_GPU_EINVAL, "unknown precision mode %d", p->precision);
+  if (p->sweep_tuning != RHYME_GPU_TUNE_AUTO && p->sweep_tuning != RHYME_GPU_TUNE_FIXED)
+    return fail(ctx, RHYME_GPU_EINVAL, "unknown sweep tuning mode %d", p->sweep_tuning);
   if (p->n_iteration < 0) return fail(ctx, RHYME_GPU_EINVAL, "n_iteration must be >= 0");
   if (!(p->gamma > 1.0)) return fail(ctx, RHYME_GPU_EINVAL, "gamma must exceed 1");
   if (!(p->kb_amu > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "kb_amu must be positive");
@@ -202,6 +208,7 @@ void make_mixed_params(const DevParams& d, MixedParams* m) {
   m->ndim = d.ndim;
   m->limiter = d.limiter;
   m->omega = (float)d.omega;
+  m->omega64 = d.omega;
 }
 
 // Frees a box's device memory in stream order on `st` (after the work
@@ -471,6 +478,105 @@ StepScratch scratch_of(Box* b, bool trace) {
 
 // One driver step on the device: dt (into s.dt), ghost fill of U (mirrored
 // into the other buffer), solve U -> other buffer.
+// ---- autotuner of the mixed sweeps ------------------------------------------
+//
+// A box-size class is (NDIM, axis, ceil(log2) of the box's extent along the
+// axis and along the pencil axis, each clamped to [3, 10]). The first box of
+// a class met by a context has its sweep along that axis timed with every
+// candidate tile shape (one warm-up and three timed launches each, CUDA
+// events on the context's stream) on its current state; the fastest shape is
+// kept for the class. A sweep only reads U^n and its FP32 mirror, so the
+// timing launches leave the state alone (they write the next-step buffers,
+// which the step itself overwrites).
+
+int size_bucket(int n) {
+  int b = 3;
+  while (b < 10 && (1 << b) < n) ++b;
+  return b;
+}
+
+int class_key(int D, int axis, const Geom& g) {
+  const int bax = (D == 1) ? 1 : (axis == 0 ? 1 : 0);
+  const int nB = (bax < D) ? g.n[bax] : 1;
+  return D | (axis << 2) | (size_bucket(g.n[axis]) << 4) | (size_bucket(nB) << 8);
+}
+
+int tune_axis(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx, int axis, int* best) {
+  const int D = ctx->params.ndim;
+  const int c = b->cur;
+  StepScratch sc = scratch_of(b, false);
+  *best = default_sweep_shape(D, axis, b->g.n[axis]);
+  CK(launch_cfl_mixed(b->mp, b->Uf[c], b->g, b->dp.courant, dx, sc, ctx->stream));
+  CK(launch_ghost_fill_f32(b->dp, b->Uf[c], b->g, ctx->stream));
+  cudaEvent_t ev[2];
+  CK(cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return fail(ctx, RHYME_GPU_ECUDA, "event create failed");
+  }
+  int rc = RHYME_GPU_OK;
+  float best_ms = 0.f;
+  bool have = false;
+  for (int k = 0; k < kSweepShapes && rc == RHYME_GPU_OK; ++k) {
+    float total = 0.f;
+    bool ok = true;
+    for (int rep = 0; rep < 4 && ok; ++rep) {
+      cudaError_t e = cudaMemsetAsync(b->fbq.n, 0, sizeof(int), ctx->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[0], ctx->stream);
+      if (e == cudaSuccess)
+        e = launch_sweep_axis(D, axis, k, b->mp, b->Uf[c], b->state[c], b->g, dx, sc.dt, b->acc,
+                              b->state[1 - c], b->Uf[1 - c], b->fbq, ctx->stream);
+      if (e == cudaErrorInvalidConfiguration) {  // grid too large for this shape
+        ok = false;
+        break;
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+      if (e != cudaSuccess) {
+        rc = fail(ctx, RHYME_GPU_ECUDA, "autotune launch: %s", cudaGetErrorString(e));
+        break;
+      }
+      rc = wait_stream(ctx);
+      if (rc != RHYME_GPU_OK) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[0], ev[1]);
+      if (rep > 0) total += ms;
+    }
+    if (rc == RHYME_GPU_OK && ok && (!have || total < best_ms)) {
+      have = true;
+      best_ms = total;
+      *best = k;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (rc == RHYME_GPU_OK) CK(cudaMemsetAsync(b->fbq.n, 0, sizeof(int), ctx->stream));
+  return rc;
+}
+
+// The box's tile shapes (mixed mode): from the class table, tuning the
+// classes not seen yet (RHYME_GPU_TUNE_AUTO), or by the size rule. Must run
+// outside stream capture.
+int box_plan(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
+  if (!ctx->mixed || b->plan_valid) return RHYME_GPU_OK;
+  const int D = ctx->params.ndim;
+  for (int a = 0; a < 3; ++a) b->plan.shape[a] = default_sweep_shape(D, a < D ? a : 0, b->g.n[a < D ? a : 0]);
+  if (ctx->params.sweep_tuning == RHYME_GPU_TUNE_AUTO) {
+    for (int a = 0; a < D; ++a) {
+      const int key = class_key(D, a, b->g);
+      auto it = ctx->tuned.find(key);
+      if (it == ctx->tuned.end()) {
+        int best = 0;
+        int rc = tune_axis(ctx, b, dx, a, &best);
+        if (rc != RHYME_GPU_OK) return rc;
+        it = ctx->tuned.emplace(key, best).first;
+      }
+      b->plan.shape[a] = it->second;
+    }
+  }
+  b->plan_valid = true;
+  return RHYME_GPU_OK;
+}
+
 cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool trace) {
   StepScratch s = scratch_of(b, trace);
   double* U = b->state[cur];
@@ -481,7 +587,7 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
     if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[cur], b->g, ctx->stream);
     if (e == cudaSuccess)
       e = launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fbq,
-                                ctx->stream);
+                                b->plan, ctx->stream);
     return e;
   }
   cudaError_t e = launch_cfl(b->dp, U, b->g, dx, s, ctx->stream);
@@ -492,6 +598,8 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
 
 int ensure_graphs(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
   if (b->graph_valid && memcmp(&b->graph_dx, &dx, sizeof(Dx)) == 0) return RHYME_GPU_OK;
+  int prc = box_plan(ctx, b, dx);
+  if (prc != RHYME_GPU_OK) return prc;
   for (int i = 0; i < 2; ++i) {
     if (b->graph[i]) {
       cudaGraphExecDestroy(b->graph[i]);
@@ -558,15 +666,17 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(ctx, RHYME_GPU_EINVAL, "dt must be positive and finite");
   Dx d = make_dx(ctx->params.ndim, dx);
+  int rc = box_plan(ctx, b, d);
+  if (rc != RHYME_GPU_OK) return rc;
   // The pinned staging scalar may still be read by an earlier copy; wait for
   // it before reuse (cheap: the stream is usually idle at this point).
-  int rc = wait_stream(ctx);
+  rc = wait_stream(ctx);
   if (rc != RHYME_GPU_OK) return rc;
   ctx->pinned_dt[0] = dt;
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->mixed)
     CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
-                             b->acc, b->g, d, scratch_of(b, false), b->fbq, ctx->stream));
+                             b->acc, b->g, d, scratch_of(b, false), b->fbq, b->plan, ctx->stream));
   else
     CK(launch_mh_solve(b->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
                        ctx->stream));
@@ -720,6 +830,8 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   Dx d = make_dx(ctx->params.ndim, dx);
+  int prc = box_plan(ctx, b, d);
+  if (prc != RHYME_GPU_OK) return prc;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
   double acc[5] = {0, 0, 0, 0, 0};
@@ -730,18 +842,16 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
     double* V = b->state[1 - b->cur];
     cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
     if (ctx->mixed) {
-      // mixed: the fused sweeps are reported under "fluxes"
+      // mixed: ms[2..4] are the x, y and z sweeps (the last one with the
+      // FP64 fix-up of the queued interfaces)
       if (e == cudaSuccess) e = launch_cfl_mixed(b->mp, b->Uf[b->cur], b->g, b->dp.courant, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
       if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
       if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[b->cur], b->g, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
-      if (e == cudaSuccess) e = cudaEventRecord(ev[3], ctx->stream);
       if (e == cudaSuccess)
         e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
-                                  b->fbq, ctx->stream);
-      if (e == cudaSuccess) e = cudaEventRecord(ev[4], ctx->stream);
-      if (e == cudaSuccess) e = cudaEventRecord(ev[5], ctx->stream);
+                                  b->fbq, b->plan, ctx->stream, ev + 3);
     } else {
       if (e == cudaSuccess) e = launch_cfl(b->dp, U, b->g, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
@@ -764,6 +874,19 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 5; ++k) ms[k] = acc[k] / nsteps;
   return rc;
+}
+
+extern "C" int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int tile_cells[3],
+                                    int tile_pencils[3]) {
+  if (!ctx || !dx || !tile_cells || !tile_pencils) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  for (int a = 0; a < 3; ++a) tile_cells[a] = tile_pencils[a] = 0;
+  if (!ctx->mixed) return RHYME_GPU_OK;
+  int rc = box_plan(ctx, b, make_dx(ctx->params.ndim, dx));
+  if (rc != RHYME_GPU_OK) return rc;
+  for (int a = 0; a < ctx->params.ndim; ++a) sweep_shape(ctx->params.ndim, b->plan.shape[a], &tile_cells[a], &tile_pencils[a]);
+  return RHYME_GPU_OK;
 }
 
 extern "C" int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count) {
@@ -798,6 +921,7 @@ extern "C" int rhyme_gpu_set_box_params(rhyme_gpu_ctx* ctx, int handle, const in
   b->dp.omega = omega;
   b->mp.limiter = limiter;
   b->mp.omega = (float)omega;
+  b->mp.omega64 = omega;
   b->graph_valid = false;
   return RHYME_GPU_OK;
 }
@@ -857,10 +981,12 @@ int batch_build(rhyme_gpu_batch* B) {
   std::vector<BoxDesc> tab[2];
   tab[0].resize(n);
   tab[1].resize(n);
-  std::vector<WorkItem> cfl, ghost, faces, flux, update, sweep[3];
+  std::vector<WorkItem> cfl, ghost, faces, flux, update, sweep[3][kSweepShapes];
   long long qcap = 0;
   for (int i = 0; i < n; ++i) {
     Box* b = ctx->boxes[B->handles[i]];
+    int rc = box_plan(ctx, b, b->dx);
+    if (rc != RHYME_GPU_OK) return rc;
     B->base_cur[i] = b->cur;
     const long long cells = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
     qcap += D * cells / 16;
@@ -905,14 +1031,9 @@ int batch_build(rhyme_gpu_batch* B) {
     for (long long c = 0; c * kBatchChunk < lines; ++c) ghost.push_back({i, 0, c});
     if (ctx->mixed) {
       for (int a = 0; a < D; ++a) {
-        int S, P;
-        sweep_tiles(D, a, g.n, &S, &P);
-        const int bax = (D == 1) ? 1 : (a == 0 ? 1 : 0);
-        const int cax = (D == 3) ? 3 - a - bax : 2;
-        const long long nA = (g.n[a] + S - 1) / S;
-        const long long nB = ((bax < D ? g.n[bax] : 1) + P - 1) / P;
-        const long long nC = (cax < D) ? g.n[cax] : 1;
-        for (long long t = 0; t < nA * nB * nC; ++t) sweep[a].push_back({i, a, t});
+        const int k = b->plan.shape[a];
+        const long long nt = sweep_tile_count(D, a, k, g.n);
+        for (long long t = 0; t < nt; ++t) sweep[a][k].push_back({i, a, t});
       }
     } else {
       for (int a = 0; a < D; ++a) {
@@ -928,9 +1049,12 @@ int batch_build(rhyme_gpu_batch* B) {
     }
   }
   std::vector<WorkItem> all;
-  size_t off[8];
-  std::vector<WorkItem>* lists[8] = {&cfl, &ghost, &faces, &flux, &update, &sweep[0], &sweep[1], &sweep[2]};
-  for (int k = 0; k < 8; ++k) {
+  constexpr int kLists = 5 + 3 * kSweepShapes;
+  size_t off[kLists];
+  std::vector<WorkItem>* lists[kLists] = {&cfl, &ghost, &faces, &flux, &update};
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < kSweepShapes; ++k) lists[5 + kSweepShapes * a + k] = &sweep[a][k];
+  for (int k = 0; k < kLists; ++k) {
     off[k] = all.size();
     all.insert(all.end(), lists[k]->begin(), lists[k]->end());
   }
@@ -940,7 +1064,7 @@ int batch_build(rhyme_gpu_batch* B) {
   }
   CK(cudaMallocAsync((void**)&B->items, sizeof(WorkItem) * std::max<size_t>(all.size(), 1), ctx->stream));
   CK(cudaMemcpyAsync(B->items, all.data(), sizeof(WorkItem) * all.size(), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMallocAsync((void**)&B->heads, 16 * sizeof(int), ctx->stream));
+  CK(cudaMallocAsync((void**)&B->heads, kBatchHeads * sizeof(int), ctx->stream));
   CK(cudaMallocAsync((void**)&B->qblock, 16 * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(B->qblock, 0, 16 * sizeof(int), ctx->stream));
   B->q.cap = 0;
@@ -957,13 +1081,16 @@ int batch_build(rhyme_gpu_batch* B) {
   L.faces = B->items + off[2];
   L.flux = B->items + off[3];
   L.update = B->items + off[4];
-  for (int a = 0; a < 3; ++a) L.sweep[a] = B->items + off[5 + a];
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < kSweepShapes; ++k) {
+      L.sweep[a][k] = B->items + off[5 + kSweepShapes * a + k];
+      L.n_sweep[a][k] = (int)sweep[a][k].size();
+    }
   L.n_cfl = (int)cfl.size();
   L.n_ghost = (int)ghost.size();
   L.n_faces = (int)faces.size();
   L.n_flux = (int)flux.size();
   L.n_update = (int)update.size();
-  for (int a = 0; a < 3; ++a) L.n_sweep[a] = (int)sweep[a].size();
   L.heads = B->heads;
   return RHYME_GPU_OK;
 }

@@ -1,0 +1,233 @@
+// sweep.cuh -- the fused per-axis sweep of the mixed-precision step.
+//
+// A CTA of kSweepThreads threads stages a slab of the FP32 mirror Uf (S
+// cells along the sweep axis plus the 2-cell ghost/halo layer, for P
+// pencils) in shared memory with coalesced loads, computes FP32 limited
+// slopes and half-step face states for S+2 cells, solves the S+1 exact
+// Riemann problems of the slab in FP32 (one thread per interface) and forms
+// the flux difference of its S cells. The tile shape (S, P) is a template
+// parameter; sweeps.cu instantiates every shape of the candidate set for
+// the autotuner, once per dimensionality.
+#pragma once
+
+#include "rgpu_internal.h"
+
+namespace rgpu {
+namespace {
+
+constexpr int kSweepThreads = 256;
+
+// Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),
+// acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
+enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
+
+// Slab geometry of axis A: pencils run along B (x unless A is x).
+template <int D, int A>
+struct Axes {
+  static constexpr int B = (D == 1) ? 1 : (A == 0 ? 1 : 0);
+  static constexpr int C = (D == 3) ? 3 - A - B : 2;
+};
+
+// Shared-memory slab; index (la along A, lb along the pencils) is stored
+// with the x-fast index innermost so consecutive threads hit consecutive
+// banks in both orientations.
+template <int D, int S, int P>
+struct SweepSmem {
+  float u[D + 2][(S + 4) * P];   // FP32 state slab (ghost/halo layer included)
+  float ul[D + 2][(S + 2) * P];  // face states, left / right
+  float ur[D + 2][(S + 2) * P];
+  float f[D + 2][(S + 1) * P];   // interface fluxes
+};
+
+// One slab (tile tA along the sweep axis, tB across the pencils, plane cC)
+// of a sweep. `box` tags queued FP64 interfaces (0 for a single box).
+template <int D, int A, int S, int P, int MODE>
+__device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, float omega,
+                                           const float* __restrict__ Uf, const double* __restrict__ U,
+                                           const Geom& g, const Dx& dx, const double* __restrict__ dtp,
+                                           float* __restrict__ acc, double* __restrict__ Unew,
+                                           float* __restrict__ Ufnew, const FallbackQueue& q, int box,
+                                           int tA, int tB, int cC, SweepSmem<D, S, P>& sh) {
+  constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
+  const int NA = g.n[A];
+  const int NB = (B < D) ? g.n[B] : 1;
+  const int a0 = tA * S + 1;  // first interior cell of the slab along A
+  const int b0 = tB * P + 1;
+  const long long F = g.field;
+  // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on GB300)
+  __shared__ float s_dtdx[2];
+  __syncthreads();  // the previous tile of this CTA is done with the smem
+  if (threadIdx.x == 0) {
+    const double dt = *dtp;
+    s_dtdx[0] = (float)(dt / dx.v[A]);
+    s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+  }
+
+  auto offset = [&](int ga, int gb) -> long long {
+    int c3[3] = {1, 1, 1};
+    c3[A] = ga;
+    if (B < D) c3[B] = gb;
+    if (C < D) c3[C] = cC;
+    return g.at(D, c3[0], c3[1], c3[2]);
+  };
+  // thread item -> (la, lb), x-fast first; ix() the matching smem index
+  auto split = [&](int it, int na, int& la, int& lb) {
+    if (A == 0) {
+      la = it % na;
+      lb = it / na;
+    } else {
+      lb = it % P;
+      la = it / P;
+    }
+  };
+  auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
+
+  // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
+  for (int it = threadIdx.x; it < (S + 4) * P; it += kSweepThreads) {
+    int la, lb;
+    split(it, S + 4, la, lb);
+    const int ga = a0 - 2 + la, gb = b0 + lb;
+    const bool ok = ga <= NA + 2 && gb <= NB;
+    const long long o = ok ? offset(ga, gb) : 0;
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) sh.u[c][ix(la, lb, S + 4)] = ok ? Uf[(long long)c * F + o] : 0.f;
+  }
+  __syncthreads();
+  const float dtdx = s_dtdx[0];
+  const float hdtdx = s_dtdx[1];
+
+  // 2. face states of cells a0-1 .. min(a0+S, NA+1)
+  for (int it = threadIdx.x; it < (S + 2) * P; it += kSweepThreads) {
+    int la, lb;
+    split(it, S + 2, la, lb);
+    if (a0 - 1 + la > NA + 1 || b0 + lb > NB) continue;
+    float um[D + 2], u0[D + 2], up[D + 2], l[D + 2], r[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      um[c] = sh.u[c][ix(la, lb, S + 4)];
+      u0[c] = sh.u[c][ix(la + 1, lb, S + 4)];
+      up[c] = sh.u[c][ix(la + 2, lb, S + 4)];
+    }
+    face_states<D, A>(M.G, limiter, omega, um, u0, up, hdtdx, l, r);
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      sh.ul[c][ix(la, lb, S + 2)] = l[c];
+      sh.ur[c][ix(la, lb, S + 2)] = r[c];
+    }
+  }
+  __syncthreads();
+
+  // 3. FP32 Riemann problems at interfaces (a0-1+li | a0+li), li in [0, S]
+  for (int it = threadIdx.x; it < (S + 1) * P; it += kSweepThreads) {
+    int li, lb;
+    split(it, S + 1, li, lb);
+    if (a0 - 1 + li > NA || b0 + lb > NB) continue;
+    float l[D + 2], r[D + 2], u[D + 2], f[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      l[c] = sh.ur[c][ix(li, lb, S + 2)];
+      r[c] = sh.ul[c][ix(li + 1, lb, S + 2)];
+    }
+    bool need64 = false;
+    rp_solve<D, A, float, true>(M.G, M.rp, l, r, 0.f, u, &need64);
+    if (!need64) {
+      flux<D, A>(M.G, u, f);
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c)
+        if (!isfinite(f[c])) need64 = true;
+    }
+    if (need64) {
+      // zero here; the FP64 correction is applied after the last sweep.
+      // Each interface is queued once: by the tile whose left face it is,
+      // or by the last tile for the box's right boundary.
+      const int ga = a0 - 1 + li;
+      if (li < S || ga == NA) {
+        const int slot = atomicAdd(q.n, 1);
+        if (slot < q.cap) {
+          FallbackEntry& e = q.e[slot];
+          e.axis = A;
+          e.ga = ga;
+          e.box = box;
+          e.o = offset(ga, b0 + lb);
+        } else {
+          atomicOr(q.status, 2);  // queue full: the interface keeps a zero flux
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c) f[c] = 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = f[c];
+  }
+  __syncthreads();
+
+  // 4. flux differences of cells a0 .. a0+S-1 and the accumulation
+  for (int it = threadIdx.x; it < S * P; it += kSweepThreads) {
+    int lu, lb;
+    split(it, S, lu, lb);
+    const int ga = a0 + lu, gb = b0 + lb;
+    if (ga > NA || gb > NB) continue;
+    const long long o = offset(ga, gb);
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const float x = dtdx * (sh.f[c][ix(lu, lb, S + 1)] - sh.f[c][ix(lu + 1, lb, S + 1)]);
+      const long long oc = (long long)c * F + o;
+      if (MODE == FIRST) {
+        acc[oc] = x;
+      } else if (MODE == MID) {
+        acc[oc] = acc[oc] + x;
+      } else {
+        const float tot = (MODE == LAST) ? acc[oc] + x : x;
+        const double un = U[oc] + (double)tot;
+        Unew[oc] = un;
+        Ufnew[oc] = (float)un;
+      }
+    }
+  }
+}
+
+template <int D, int A, int S, int P, int MODE>
+__global__ void __launch_bounds__(kSweepThreads, 4)
+    sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
+                 Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
+                 double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
+  constexpr int C = Axes<D, A>::C;
+  __shared__ SweepSmem<D, S, P> sh;
+  // tile origin: the fast grid axis runs along x
+  const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
+  const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
+  const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
+  sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, 0, tA, tB, cC,
+                               sh);
+}
+
+// The same sweep over the tiles of a batch of boxes, taken from a work queue
+// (item.chunk = the tile's linear index tA + nA * (tB + nB * (cC - 1))).
+template <int D, int A, int S, int P, int MODE>
+__global__ void __launch_bounds__(kSweepThreads, 4)
+    batch_sweep_kernel(MixedParams M, const BoxDesc* __restrict__ TB, const WorkItem* __restrict__ items,
+                       int n, int* head, FallbackQueue q) {
+  constexpr int B = Axes<D, A>::B;
+  __shared__ SweepSmem<D, S, P> sh;
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n) break;
+    const WorkItem w = items[it];
+    const BoxDesc& b = TB[w.box];
+    const int nA = (b.g.n[A] + S - 1) / S;
+    const int nB = ((B < D ? b.g.n[B] : 1) + P - 1) / P;
+    const int tA = (int)(w.chunk % nA);
+    const long long r = w.chunk / nA;
+    const int tB = (int)(r % nB);
+    const int cC = (int)(r / nB) + 1;
+    sweep_tile<D, A, S, P, MODE>(M, b.limiter, b.omega_f, b.Uf, b.U, b.g, b.dx, b.ctl, b.acc, b.V, b.Vf,
+                                 q, w.box, tA, tB, cC, sh);
+  }
+}
+
+}  // namespace
+}  // namespace rgpu

@@ -1,0 +1,127 @@
+// sweeps.cu -- launchers of the mixed sweeps for every axis and tile shape of
+// one dimensionality. Compiled three times (-DSWEEP_D=1, 2, 3) so the
+// instantiations (axes x candidate shapes, single box and batched) build in
+// parallel.
+#include "sweep.cuh"
+
+#ifndef SWEEP_D
+#error "compile once per dimensionality with -DSWEEP_D=1, 2 or 3"
+#endif
+
+namespace rgpu {
+namespace {
+
+// The accumulation mode of an axis: the first axis starts the FP32 sum, the
+// last one adds it to U^n in FP64.
+template <int D, int A>
+constexpr int mode_of() {
+  return D == 1 ? ONLY : (A == 0 ? FIRST : (A == D - 1 ? LAST : MID));
+}
+
+template <int D, int A, int S, int P>
+cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, const Geom& g, const Dx& dx,
+                       const double* dtp, float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,
+                       cudaStream_t st) {
+  constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
+  const int NA = g.n[A];
+  const int NB = (B < D) ? g.n[B] : 1;
+  const int NC = (C < D) ? g.n[C] : 1;
+  const int tA = (NA + S - 1) / S, tB = (NB + P - 1) / P;
+  if ((A == 0 ? tB : tA) > 65535 || NC > 65535) return cudaErrorInvalidConfiguration;
+  const dim3 grid = (A == 0) ? dim3(tA, tB, NC) : dim3(tB, tA, NC);
+  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, kSweepThreads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew,
+                                                                             Ufnew, q);
+  return cudaGetLastError();
+}
+
+template <int D, int A, int S, int P>
+cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const WorkItem* items, int n, int* head,
+                             const FallbackQueue& q, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  batch_sweep_kernel<D, A, S, P, mode_of<D, A>()><<<152 * 4, kSweepThreads, 0, st>>>(M, TB, items, n, head, q);
+  return cudaGetLastError();
+}
+
+// shape index -> (S, P) as in sweep_shape()
+template <int D, int A>
+cudaError_t by_shape(int shape, const MixedParams& M, const float* Uf, const double* U, const Geom& g,
+                     const Dx& dx, const double* dtp, float* acc, double* Unew, float* Ufnew,
+                     const FallbackQueue& q, cudaStream_t st) {
+  if constexpr (D == 1) {
+    switch (shape) {
+      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    }
+  } else {
+    switch (shape) {
+      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int D, int A>
+cudaError_t batch_by_shape(int shape, const MixedParams& M, const BoxDesc* TB, const WorkItem* items, int n,
+                           int* head, const FallbackQueue& q, cudaStream_t st) {
+  if constexpr (D == 1) {
+    switch (shape) {
+      case 0: return launch_batch_one<D, A, 64, 1>(M, TB, items, n, head, q, st);
+      case 1: return launch_batch_one<D, A, 128, 1>(M, TB, items, n, head, q, st);
+      case 2: return launch_batch_one<D, A, 256, 1>(M, TB, items, n, head, q, st);
+      case 3: return launch_batch_one<D, A, 512, 1>(M, TB, items, n, head, q, st);
+    }
+  } else {
+    switch (shape) {
+      case 0: return launch_batch_one<D, A, 8, 32>(M, TB, items, n, head, q, st);
+      case 1: return launch_batch_one<D, A, 16, 16>(M, TB, items, n, head, q, st);
+      case 2: return launch_batch_one<D, A, 32, 8>(M, TB, items, n, head, q, st);
+      case 3: return launch_batch_one<D, A, 64, 4>(M, TB, items, n, head, q, st);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+#define RGPU_CAT2(a, b) a##b
+#define RGPU_CAT(a, b) RGPU_CAT2(a, b)
+
+cudaError_t RGPU_CAT(launch_sweep_axis_, SWEEP_D)(int axis, int shape, const MixedParams& M, const float* Uf,
+                                                 const double* U, const Geom& g, const Dx& dx,
+                                                 const double* dtp, float* acc, double* Unew, float* Ufnew,
+                                                 const FallbackQueue& q, cudaStream_t st) {
+  constexpr int D = SWEEP_D;
+  switch (axis) {
+    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    case 1:
+      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      break;
+    case 2:
+      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      break;
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t RGPU_CAT(launch_batch_sweep_axis_, SWEEP_D)(int axis, int shape, const MixedParams& M,
+                                                       const BoxDesc* TB, const WorkItem* items, int n,
+                                                       int* head, const FallbackQueue& q, cudaStream_t st) {
+  constexpr int D = SWEEP_D;
+  switch (axis) {
+    case 0: return batch_by_shape<D, 0>(shape, M, TB, items, n, head, q, st);
+    case 1:
+      if constexpr (D > 1) return batch_by_shape<D, 1>(shape, M, TB, items, n, head, q, st);
+      break;
+    case 2:
+      if constexpr (D > 2) return batch_by_shape<D, 2>(shape, M, TB, items, n, head, q, st);
+      break;
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace rgpu

@@ -19,6 +19,8 @@ module rhyme_gpu_c
 
    integer(c_int), parameter :: rhyme_gpu_fp64 = 0
    integer(c_int), parameter :: rhyme_gpu_mixed = 1
+   integer(c_int), parameter :: rhyme_gpu_tune_auto = 0
+   integer(c_int), parameter :: rhyme_gpu_tune_fixed = 1
 
    type, bind(c) :: rhyme_gpu_params_t
       integer(c_int) :: ndim = 0
@@ -27,7 +29,7 @@ module rhyme_gpu_c
       integer(c_int) :: solver_type = 0
       integer(c_int) :: bc(6) = 0
       integer(c_int) :: precision = 0
-      integer(c_int) :: reserved = 0
+      integer(c_int) :: sweep_tuning = 0
       real(c_double) :: gamma = 0d0
       real(c_double) :: kb_amu = 0d0
       real(c_double) :: courant = 0d0

@@ -35,7 +35,7 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
            "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
            "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
-           "rhyme_gpu_server_destroy"]
+           "rhyme_gpu_server_destroy", "rhyme_gpu_sweep_plan"]
 REQ_PENDING, REQ_ACTIVE, REQ_DRAINING, REQ_DONE = 0, 1, 2, 3
 
 
@@ -45,6 +45,7 @@ class Request(C.Structure):
                 ("bc", C.c_int * 6), ("omega", C.c_double), ("dx", C.c_double * 3),
                 ("cells", C.POINTER(C.c_double))]
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
+PHASES_MIXED = ["cfl", "ghost_fill", "sweep_x", "sweep_y", "sweep_z"]
 
 
 class RhymeGpuError(RuntimeError):
@@ -57,7 +58,7 @@ class Params(C.Structure):
     """struct rhyme_gpu_params (include/rhyme_gpu.h)."""
     _fields_ = [("ndim", C.c_int), ("limiter", C.c_int), ("n_iteration", C.c_int),
                 ("solver_type", C.c_int), ("bc", C.c_int * 6), ("precision", C.c_int),
-                ("reserved", C.c_int), ("gamma", C.c_double), ("kb_amu", C.c_double),
+                ("sweep_tuning", C.c_int), ("gamma", C.c_double), ("kb_amu", C.c_double),
                 ("courant", C.c_double), ("omega", C.c_double), ("vacuum_density", C.c_double),
                 ("vacuum_pressure", C.c_double), ("tolerance", C.c_double),
                 ("inflow", (C.c_double * 5) * 6)]
@@ -72,6 +73,7 @@ def params_struct(p):
     for i, b in enumerate(p["bc"]):
         s.bc[i] = b
     s.precision = p.get("precision", 0)
+    s.sweep_tuning = p.get("sweep_tuning", 0)
     s.gamma = p["gamma"]
     s.kb_amu = p["kb_amu"]
     s.courant = p["courant"]
@@ -123,6 +125,7 @@ def load():
     L.rhyme_gpu_profile_steps.argtypes = [vp, C.c_int, dp, C.c_int, dp]
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
+    L.rhyme_gpu_sweep_plan.argtypes = [vp, C.c_int, dp, ip, ip]
     L.rhyme_gpu_mh_solve_noalloc.argtypes = [C.POINTER(Params), vp, vp, ip, dp, C.c_double, vp]
     L.rhyme_gpu_set_box_params.argtypes = [vp, C.c_int, ip, C.c_int, C.c_double]
     L.rhyme_gpu_batch_create.argtypes = [vp, ip, dp, C.c_int, C.POINTER(vp)]
@@ -278,6 +281,16 @@ class Context:
         self._check(self.lib.rhyme_gpu_fallback_count(self.h, box.handle, C.byref(n)))
         return n.value
 
+    def sweep_plan(self, box, dx):
+        """[(cells along the axis, pencils)] per axis of the box's mixed
+        sweeps (empty in FP64 mode)."""
+        s = np.zeros(3, dtype=np.int32)
+        p = np.zeros(3, dtype=np.int32)
+        self._check(self.lib.rhyme_gpu_sweep_plan(self.h, box.handle, _d(_dx3(dx)),
+                                                  s.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  p.ctypes.data_as(C.POINTER(C.c_int))))
+        return [(int(a), int(b)) for a, b in zip(s, p) if a]
+
     def synchronize(self):
         self._check(self.lib.rhyme_gpu_synchronize(self.h))
 
@@ -317,10 +330,12 @@ class Context:
         return dts[:nsteps] if trace else None
 
     def profile_steps(self, box, dx, nsteps):
-        """Mean ms per launch of each phase (PHASES) over nsteps steps."""
+        """Mean ms per step of each phase (PHASES, or PHASES_MIXED in mixed
+        precision) over nsteps steps."""
         ms = np.zeros(5)
         self._check(self.lib.rhyme_gpu_profile_steps(self.h, box.handle, _d(_dx3(dx)), int(nsteps), _d(ms)))
-        return dict(zip(PHASES, ms.tolist()))
+        names = PHASES_MIXED if self._p.precision == 1 else PHASES
+        return dict(zip(names, ms.tolist()))
 
     # ---- element-level interfaces --------------------------------------
     def riemann_problem_solve(self, l, r, dx, dt, axis):

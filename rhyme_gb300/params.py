@@ -34,7 +34,7 @@ KB_AMU_SI = float(np.float64(np.float32(1.38064852e-23)) /
 def hydro_params(ndim, limiter=MINMOD, bc=(OUTFLOW,) * 6, gamma=GAMMA["monatomic"],
                  courant=0.8, omega=0.0, vac_rho=0.0, vac_p=0.0, tol=1e-6,
                  n_iter=100, solver_type=MEMORY_INTENSIVE, kb_amu=KB_AMU_SI,
-                 precision=FP64, inflow=None):
+                 precision=FP64, inflow=None, sweep_tuning=0):
     """The values Rhyme's modules hold for one run, as one mapping."""
     bc = list(bc) + [OUTFLOW] * (6 - len(bc))
     return dict(ndim=int(ndim), gamma=float(gamma), kb_amu=float(kb_amu),
@@ -42,4 +42,4 @@ def hydro_params(ndim, limiter=MINMOD, bc=(OUTFLOW,) * 6, gamma=GAMMA["monatomic
                 vac_rho=float(vac_rho), vac_p=float(vac_p), tol=float(tol),
                 n_iter=int(n_iter), bc=[int(b) for b in bc[:6]],
                 solver_type=int(solver_type), precision=int(precision),
-                inflow=inflow)
+                inflow=inflow, sweep_tuning=int(sweep_tuning))

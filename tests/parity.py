@@ -7,26 +7,10 @@ The plain FP64 bar is 1e-12 for both, and 1e-14 relative for each dt.
 """
 import numpy as np
 
+from rhyme_gb300.metrics import field_errors, interior  # noqa: F401
+
 FP64_FIELD_TOL = 1e-12
 FP64_DT_TOL = 1e-14
-
-
-def interior(cells, ndim):
-    return cells[(slice(None),) + (slice(2, -2),) * ndim]
-
-
-def field_errors(gpu_cells, ref_cells, ndim):
-    a = interior(gpu_cells, ndim)
-    b = interior(ref_cells, ndim)
-    out = []
-    for c in range(ndim + 2):
-        d = np.abs(a[c] - b[c])
-        s1 = np.abs(b[c]).sum()
-        sm = np.abs(b[c]).max()
-        l1 = d.sum() / s1 if s1 > 0 else d.sum()
-        li = d.max() / sm if sm > 0 else d.max()
-        out.append((float(l1), float(li)))
-    return out
 
 
 def assert_fp64_parity(gpu_cells, ref_cells, ndim, dts_gpu=None, dts_ref=None,

