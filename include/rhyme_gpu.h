@@ -205,6 +205,113 @@ int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
 int rhyme_gpu_fallback_count(rhyme_gpu_ctx* ctx, int handle, long long* count);
 
 /*
+ * Chombo output drain: replaces the packing loop of
+ * rhyme_chombo_write_level_data.f90:36-70 for the hydro components. Packs
+ * the interior cells of the listed boxes (their current state), box after
+ * box and component after component, in Fortran order and converted to
+ * FP32, into `data` in the layout of the level's "data:datatype=0" dataset:
+ * box b starts at sum over the boxes before it of prod(dims) * ncmp, its
+ * component c at + c * prod(dims). Only components 1..NDIM+2 are written;
+ * the blocks of the other ncmp - NDIM - 2 components (temperature, species
+ * fractions, which stay on the host) are left untouched. Asynchronous: the
+ * pack runs after the work already queued on the context's stream and the
+ * copy on a copy stream; `data` (capacity in floats) must stay valid until
+ * rhyme_gpu_output_wait returns (page-locked memory keeps the copy off the
+ * host's critical path). A second output waits for the first.
+ */
+int rhyme_gpu_output_level(rhyme_gpu_ctx* ctx, const int* handles, int n, int ncmp, float* data,
+                           long long capacity);
+int rhyme_gpu_output_wait(rhyme_gpu_ctx* ctx);
+
+/*
+ * Conservation totals, rhyme_samr_calc_total_mass.f90 and
+ * rhyme_samr_calc_total_energy.f90 on the device: totals[0] = sum of rho
+ * where rho > 0 and totals[1] = sum of e_tot where e_tot > 0 over every
+ * cell of the box, ghosts included (the reference then multiplies by
+ * product(box_lengths)). Summed in double-double and rounded once.
+ */
+int rhyme_gpu_box_totals(rhyme_gpu_ctx* ctx, int handle, double totals[2]);
+
+/*
+ * Sanity checks on the device: the general checks of
+ * rhyme_sanity_check_perform.f90:34-90 and the property statistics of
+ * rhyme_sanity_check_fill.f90:75-185 for the properties that live on the
+ * device (rho, vx, vy, vz, e_tot, |v|, Mach), over the interior cells.
+ * Per property: in range[2] and enabled (sc%<p>_range, sc%properties);
+ * out the counts below / above the range, the lowest value below it and
+ * the highest above it with their first 1-based cells in Fortran loop
+ * order, and the running extreme the loop held just before reaching them
+ * (the reference's vbelow(1) / vabove(1) within this call; +-DBL_MAX when
+ * none). The reference keeps vbelow/vabove across calls; a caller merges
+ * with its kept values (a new extreme replaces them only if beyond them).
+ * Mach is |v| / cs of the cell's own state (the reference passes the slice
+ * rho_u:e_tot to calc_cs, which reads one component past it).
+ */
+enum { RHYME_GPU_SC_RHO = 0, RHYME_GPU_SC_VX, RHYME_GPU_SC_VY, RHYME_GPU_SC_VZ, RHYME_GPU_SC_E_TOT,
+       RHYME_GPU_SC_ABS_V, RHYME_GPU_SC_MACH, RHYME_GPU_SC_COUNT };
+
+typedef struct rhyme_gpu_sanity_property {
+  double range[2];
+  int enabled;
+  int reserved;
+  long long nbelow, nabove;
+  double vbelow, vbelow_prev;
+  double vabove, vabove_prev;
+  int cbelow[3], cabove[3];
+} rhyme_gpu_sanity_property;
+
+typedef struct rhyme_gpu_sanity_report {
+  rhyme_gpu_sanity_property prop[RHYME_GPU_SC_COUNT];
+  int nan[5];          /* a NaN in component c (rho, rho_u, [rho_v, [rho_w,]] e_tot) */
+  int reserved;
+  double rho_min, e_tot_min;           /* minval over the interior (negative: the warnings) */
+  int rho_min_at[3], e_tot_min_at[3];  /* minloc, 1-based */
+} rhyme_gpu_sanity_report;
+
+int rhyme_gpu_sanity_check(rhyme_gpu_ctx* ctx, int handle, rhyme_gpu_sanity_report* report);
+
+/*
+ * Initial conditions painted on the device: the hydro part of
+ * rhyme_drawing_init.f90:20-78. The shapes are applied in order (a canvas
+ * or shape overwrites the cells it covers; without a canvas the cells keep
+ * their values, the reference's transparent canvas), then every perturbation
+ * is summed per cell and added once as a conserved vector
+ * (rhyme_drawing_apply_perturbations.f90). Colours and bases are primitive
+ * (rho, u, v, w, p); lengths are in level-0 cells. A sphere blends its two
+ * colours over every cell of the box, as the reference does, so a second
+ * sphere repaints the first one's outside. Extensions, off when 0:
+ * `periodic` (a sphere also covers the box's periodic images), sigma = 0 for
+ * a sphere (sharp edge, dist < r), `keep_outside` (a sharp sphere leaves the
+ * cells outside it alone, so several spheres can be drawn), `phase` (of a
+ * harmonic). Not painted on
+ * the device: the power-law canvas, smooth cuboids, prisms and white noise
+ * (the reference draws it from the Fortran generator).
+ */
+enum { RHYME_GPU_DRAW_CANVAS = 0, RHYME_GPU_DRAW_SHARP_CUBOID = 1, RHYME_GPU_DRAW_SPHERE = 2,
+       RHYME_GPU_DRAW_SMOOTHED_SLAB = 3, RHYME_GPU_DRAW_HARMONIC = 4, RHYME_GPU_DRAW_SYMMETRIC_DECAYING = 5 };
+
+typedef struct rhyme_gpu_shape {
+  int type;            /* RHYME_GPU_DRAW_* */
+  int axis;            /* slab / perturbation axis (0 = x) */
+  int periodic;        /* sphere: nearest periodic image */
+  int keep_outside;    /* sharp sphere: cells outside keep their values */
+  int left_corner[3];  /* sharp cuboid: shape%cuboid%left_corner, lengths */
+  int lengths[3];
+  double prim[2][5];   /* colours: [0] canvas, cuboid, sphere inside, slab outside;
+                          [1] sphere outside, slab inside */
+  double origin[3];    /* sphere centre (cells) */
+  double r, sigma;     /* sphere radius and tanh width; symmetric decaying: sigma */
+  double pos[2];       /* slab edges; symmetric decaying: pos[0] */
+  double slab_sigma[2];
+  double amplitude, wavelength, phase;  /* perturbation A, lambda (cells), phase */
+  double base[5];      /* perturbation base */
+} rhyme_gpu_shape;
+
+/* left_edge: the box's left edge in level-0 cells (1 for a single box). */
+int rhyme_gpu_paint(rhyme_gpu_ctx* ctx, int handle, const int left_edge[3], const rhyme_gpu_shape* shapes,
+                    int n);
+
+/*
  * Instrumentation (no reference counterpart): the tile shape of each axis of
  * the box's mixed-precision sweeps (cells along the axis, pencils), as the
  * autotuner or the size rule chose it; tunes the box's size classes first
@@ -296,6 +403,14 @@ typedef struct rhyme_gpu_request {
   double omega;
   double dx[3];
   double* cells;  /* host, NDIM+2 ghosted blocks: initial state in, result out */
+  float* output;  /* optional (NULL): the result as a one-box level output in the
+                     Chombo "data:datatype=0" layout (FP32, NDIM+2 components,
+                     interior cells), drained like rhyme_gpu_output_level */
+  const struct rhyme_gpu_shape* shapes;  /* optional: paint the initial state on the
+                                            device (rhyme_gpu_paint, from zero cells)
+                                            instead of uploading `cells` */
+  int nshapes;
+  int reserved;
 } rhyme_gpu_request;
 
 typedef struct rhyme_gpu_server rhyme_gpu_server;

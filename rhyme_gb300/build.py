@@ -34,6 +34,9 @@ UNITS = [
     ("sweeps_3d", "sweeps.cu", ["-DSWEEP_D=3"]),
     ("noalloc", "noalloc.cu", ["--fmad=false"]),
     ("kernels_batch", "kernels_batch.cu", ["--fmad=false"]),
+    ("kernels_output", "kernels_output.cu", []),
+    ("kernels_sanity", "kernels_sanity.cu", ["--fmad=false"]),
+    ("kernels_paint", "kernels_paint.cu", ["--fmad=false"]),
 ]
 HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "box_elems.cuh", "sweep.cuh"]
 

@@ -25,6 +25,8 @@
 //
 // The CFL maximum of the mixed path is taken in FP32 over Uf; dt itself is
 // formed in FP64.
+#include <math_constants.h>
+
 #include "rgpu_internal.h"
 
 namespace rgpu {
@@ -147,6 +149,16 @@ __device__ __noinline__ void redo_interface(const MixedParams& M, int limiter, d
     w1[c] = p[0];
     w2[c] = p[sa];
     w3[c] = p[2 * sa];
+  }
+  // a non-finite U^n (a box the scheme has already lost) makes the FP64
+  // solve iterate to its cap for a NaN result: give the NaN directly
+  bool finite = true;
+#pragma unroll
+  for (int c = 0; c < D + 2; ++c) finite = finite && isfinite(w0[c]) && isfinite(w1[c]) && isfinite(w2[c]) && isfinite(w3[c]);
+  if (!finite) {
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) f[c] = CUDART_NAN;
+    return;
   }
   double lo[D + 2], ro[D + 2], l1[D + 2], r1[D + 2];
   face_states<D, AX>(M.G64, limiter, omega, w0, w1, w2, hdtdx, lo, ro);
@@ -387,10 +399,10 @@ long long sweep_tile_count(int ndim, int axis, int shape, const int* n) {
   sweep_shape(ndim, shape, &S, &P);
   const int bax = (ndim == 1) ? 1 : (axis == 0 ? 1 : 0);
   const int cax = (ndim == 3) ? 3 - axis - bax : 2;
-  const long long nA = (n[axis] + S - 1) / S;
-  const long long nB = ((bax < ndim ? n[bax] : 1) + P - 1) / P;
+  const long long nB = (bax < ndim) ? n[bax] : 1;
   const long long nC = (cax < ndim) ? n[cax] : 1;
-  return nA * nB * nC;
+  const long long nA = (n[axis] + S - 1) / S;
+  return nA * ((nB + P - 1) / P) * nC;
 }
 
 cudaError_t launch_batch_cfl_mixed(const MixedParams& M, double courant, const BoxDesc* TB,

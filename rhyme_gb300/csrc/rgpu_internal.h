@@ -69,9 +69,9 @@ __host__ __device__ inline void sweep_shape(int ndim, int shape, int* S, int* P)
   }
 }
 
-// Shape used without tuning: the smallest S that covers the box along the
-// axis, up to 32 along x (pencils stay 8 cells wide) and 16 along y and z
-// (pencils along x stay 16 cells wide, for coalescing); 256 cells in 1-D.
+// Shape used without tuning: the smallest tile S that covers the box along
+// the axis, up to 32 along x (pencils stay 8 cells wide) and 16 along y and
+// z (pencils along x stay 16 cells wide, for coalescing); 256 cells in 1-D.
 inline int default_sweep_shape(int ndim, int axis, int nA) {
   if (ndim == 1) return 2;
   const int cap = (axis == 0) ? 2 : 1;
@@ -247,7 +247,7 @@ cudaError_t launch_batch_step(const DevParams& P, const MixedParams& M, bool mix
                               cudaStream_t st);
 
 // Queue heads of a batch step: 0 cfl, 1 ghost, 2 faces, 3 flux, 4 update,
-// 5 ghost (FP32 mirror), 6 + 4 * axis + shape the sweeps.
+// 5 ghost (FP32 mirror), 6 + kSweepShapes * axis + shape the sweeps.
 constexpr int kBatchHeads = 32;
 constexpr int kHeadGhostF32 = 5;
 constexpr int kHeadSweep0 = 6;
@@ -255,6 +255,67 @@ constexpr int kHeadSweep0 = 6;
 // Chunk sizes of the batched passes (elements per work item).
 constexpr int kBatchChunk = 256;
 constexpr int kBatchFluxChunk = 128;
+
+// One box of a level output (kernels_output.cu): its current state, its
+// interior cell count, the start of its hydro elements in the flattened
+// list of all boxes' hydro elements, and its offset in the output dataset
+// (sum over the boxes before it of cells x NCMP).
+struct PackDesc {
+  const double* U;
+  Geom g;
+  long long cells;
+  long long hydro_off;
+  long long out_off;
+};
+
+cudaError_t launch_pack_level(const PackDesc* desc, int n, long long total, int ndim, float* out,
+                              cudaStream_t st);
+
+// Sanity checks (kernels_sanity.cu): the properties of
+// rhyme_sanity_check_fill.f90 that live on the device, their ranges, and
+// the partial result of a run of cells in loop order.
+enum { SC_RHO = 0, SC_VX, SC_VY, SC_VZ, SC_E_TOT, SC_ABS_V, SC_MACH, SC_COUNT };
+
+struct SanityRanges {
+  double range[SC_COUNT][2];
+  int enabled[SC_COUNT];
+};
+
+struct SanityPartial {
+  long long nbelow[SC_COUNT], nabove[SC_COUNT];
+  double vbelow[SC_COUNT], pbelow[SC_COUNT];  // extreme below the range, running extreme before it
+  double vabove[SC_COUNT], pabove[SC_COUNT];
+  long long ibelow[SC_COUNT], iabove[SC_COUNT];  // loop-order cell index of the extremes (-1: none)
+  int nan[5];                                    // a NaN in component c
+  double rho_min, e_min;                         // minima of rho and e_tot
+  long long irho_min, ie_min;                    // their first cells
+};
+
+__host__ __device__ void merge_partial(SanityPartial& a, const SanityPartial& b);
+cudaError_t launch_sanity(int ndim, const double* U, const Geom& g, const Gas<double>& G, const SanityRanges& R,
+                          SanityPartial* parts, int nblocks, SanityPartial* out, cudaStream_t st);
+// parts: 2 * nblocks double-double pairs (32 bytes each)
+cudaError_t launch_totals(int ndim, const double* U, long long field, void* parts, int nblocks, double* out,
+                          cudaStream_t st);
+
+// Initial-condition painting (kernels_paint.cu). Colours and perturbation
+// bases are primitive vectors packed as (rho, v_1..v_NDIM, p).
+enum { PAINT_CANVAS = 0, PAINT_SHARP_CUBOID, PAINT_SPHERE, PAINT_SMOOTHED_SLAB, PAINT_HARMONIC,
+       PAINT_SYMMETRIC_DECAYING };
+
+struct PaintShape {
+  int type, axis, periodic, keep_outside;
+  int lb[3], ub[3];  // sharp cuboid: cell bounds in this box (1-based, inclusive)
+  double prim[2][5];
+  double origin[3];
+  double r, sigma;
+  double pos[2], slab_sigma[2];
+  double amplitude, wavelength, phase;
+  double base[5];
+};
+
+cudaError_t launch_paint(int ndim, const PaintShape* shapes, int n, const Gas<double>& G, const Geom& g,
+                         const int* left_edge, double* U, float* Uf, cudaStream_t st);
 
 // Element-level launchers (kernels_elem.cu): device arrays in and out.
 cudaError_t launch_riemann_solve(const DevParams& P, const double* l, const double* r, long long n,

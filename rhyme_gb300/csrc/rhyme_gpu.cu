@@ -68,6 +68,14 @@ struct rhyme_gpu_ctx {
   size_t elem_cap = 0;
   double timeout_s = 600.0;
   std::map<int, int> tuned;  // box-size class -> tile shape (mixed sweeps)
+  // level output drain (rhyme_gpu_output_level)
+  cudaStream_t copy = nullptr;
+  cudaEvent_t out_packed = nullptr, out_done = nullptr;
+  float* out_dev = nullptr;
+  size_t out_cap = 0;  // floats
+  PackDesc* out_desc = nullptr;
+  size_t desc_cap = 0;  // descriptors
+  bool out_pending = false;
 };
 
 namespace {
@@ -279,7 +287,13 @@ int rhyme_gpu_destroy(rhyme_gpu_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (Box* b : ctx->boxes) destroy_box(b, ctx->stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->copy) cudaStreamSynchronize(ctx->copy);
   cudaFree(ctx->elem_buf);
+  cudaFree(ctx->out_dev);
+  cudaFree(ctx->out_desc);
+  if (ctx->out_packed) cudaEventDestroy(ctx->out_packed);
+  if (ctx->out_done) cudaEventDestroy(ctx->out_done);
+  if (ctx->copy) cudaStreamDestroy(ctx->copy);
   cudaFreeHost(ctx->pinned_dt);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -876,6 +890,261 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   return rc;
 }
 
+// ---- level output drain -----------------------------------------------------
+
+namespace {
+
+// Polls an event against the context's deadline.
+int wait_event(rhyme_gpu_ctx* ctx, cudaEvent_t ev) {
+  auto t0 = std::chrono::steady_clock::now();
+  int spins = 0;
+  for (;;) {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return RHYME_GPU_OK;
+    if (e != cudaErrorNotReady) return fail(ctx, RHYME_GPU_ECUDA, "event wait: %s", cudaGetErrorString(e));
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > ctx->timeout_s) return fail(ctx, RHYME_GPU_ETIMEDOUT, "event wait exceeded %.0f s", ctx->timeout_s);
+    if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+}  // namespace
+
+extern "C" int rhyme_gpu_output_level(rhyme_gpu_ctx* ctx, const int* handles, int n, int ncmp, float* data,
+                                      long long capacity) {
+  if (!ctx || !handles || !data || n < 1) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  const int D = ctx->params.ndim;
+  if (ncmp < D + 2) return fail(ctx, RHYME_GPU_EINVAL, "ncmp %d < NDIM+2", ncmp);
+  std::vector<PackDesc> desc(n);
+  long long out_len = 0, hydro = 0;
+  for (int i = 0; i < n; ++i) {
+    Box* b = find_box(ctx, handles[i]);
+    if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handles[i]);
+    PackDesc& d = desc[i];
+    d.U = b->state[b->cur];
+    d.g = b->g;
+    d.cells = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+    d.hydro_off = hydro;
+    d.out_off = out_len;
+    hydro += (D + 2) * d.cells;
+    out_len += (long long)ncmp * d.cells;
+  }
+  if (capacity < out_len)
+    return fail(ctx, RHYME_GPU_EINVAL, "output holds %lld values, the level needs %lld", capacity, out_len);
+  if (!ctx->copy) {
+    CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->out_packed, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->out_done, cudaEventDisableTiming));
+  }
+  // the staging buffers of an earlier output are reused once its copies ended
+  if (ctx->out_pending) {
+    int rc = wait_event(ctx, ctx->out_done);
+    if (rc != RHYME_GPU_OK) return rc;
+    ctx->out_pending = false;
+  }
+  if ((size_t)out_len > ctx->out_cap) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->out_dev);
+    ctx->out_dev = nullptr;
+    ctx->out_cap = 0;
+    CK(cudaMalloc((void**)&ctx->out_dev, sizeof(float) * (size_t)out_len));
+    ctx->out_cap = (size_t)out_len;
+  }
+  if ((size_t)n > ctx->desc_cap) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->out_desc);
+    ctx->out_desc = nullptr;
+    ctx->desc_cap = 0;
+    CK(cudaMalloc((void**)&ctx->out_desc, sizeof(PackDesc) * (size_t)n));
+    ctx->desc_cap = (size_t)n;
+  }
+  // pageable source: the copy is staged before the call returns
+  CK(cudaMemcpyAsync(ctx->out_desc, desc.data(), sizeof(PackDesc) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_pack_level(ctx->out_desc, n, hydro, D, ctx->out_dev, ctx->stream));
+  CK(cudaEventRecord(ctx->out_packed, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->copy, ctx->out_packed, 0));
+  if (ncmp == D + 2) {
+    CK(cudaMemcpyAsync(data, ctx->out_dev, sizeof(float) * (size_t)out_len, cudaMemcpyDeviceToHost, ctx->copy));
+  } else {  // the hydro blocks of a box are contiguous; the other components stay as they are
+    for (int i = 0; i < n; ++i)
+      CK(cudaMemcpyAsync(data + desc[i].out_off, ctx->out_dev + desc[i].out_off,
+                         sizeof(float) * (size_t)(D + 2) * desc[i].cells, cudaMemcpyDeviceToHost, ctx->copy));
+  }
+  CK(cudaEventRecord(ctx->out_done, ctx->copy));
+  ctx->out_pending = true;
+  return RHYME_GPU_OK;
+}
+
+extern "C" int rhyme_gpu_output_wait(rhyme_gpu_ctx* ctx) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  if (!ctx->out_pending) return RHYME_GPU_OK;
+  int rc = wait_event(ctx, ctx->out_done);
+  if (rc == RHYME_GPU_OK) ctx->out_pending = false;
+  return rc;
+}
+
+// ---- conservation totals and sanity checks ---------------------------------
+
+extern "C" int rhyme_gpu_box_totals(rhyme_gpu_ctx* ctx, int handle, double totals[2]) {
+  if (!ctx || !totals) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  const int nb = 152 * 2;
+  void* parts = nullptr;
+  double* out = nullptr;
+  CK(cudaMallocAsync(&parts, 2 * nb * 2 * sizeof(double), ctx->stream));
+  CK(cudaMallocAsync((void**)&out, 2 * sizeof(double), ctx->stream));
+  cudaError_t e = launch_totals(ctx->params.ndim, b->state[b->cur], b->g.field, parts, nb, out, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ctx->pinned_dt, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaFreeAsync(parts, ctx->stream);
+  cudaFreeAsync(out, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, RHYME_GPU_ECUDA, "totals: %s", cudaGetErrorString(e));
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  totals[0] = ctx->pinned_dt[0];
+  totals[1] = ctx->pinned_dt[1];
+  return RHYME_GPU_OK;
+}
+
+extern "C" int rhyme_gpu_sanity_check(rhyme_gpu_ctx* ctx, int handle, rhyme_gpu_sanity_report* rep) {
+  if (!ctx || !rep) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  const int D = ctx->params.ndim;
+  SanityRanges R;
+  for (int p = 0; p < SC_COUNT; ++p) {
+    R.range[p][0] = rep->prop[p].range[0];
+    R.range[p][1] = rep->prop[p].range[1];
+    R.enabled[p] = rep->prop[p].enabled ? 1 : 0;
+  }
+  if (D < 2) R.enabled[SC_VY] = 0;
+  if (D < 3) R.enabled[SC_VZ] = 0;
+  const long long total = (long long)b->g.n[0] * b->g.n[1] * b->g.n[2];
+  int nb = (int)std::min<long long>(152 * 2, (total + 255) / 256);
+  if (nb < 1) nb = 1;
+  SanityPartial* parts = nullptr;
+  SanityPartial* out = nullptr;
+  CK(cudaMallocAsync((void**)&parts, sizeof(SanityPartial) * nb, ctx->stream));
+  CK(cudaMallocAsync((void**)&out, sizeof(SanityPartial), ctx->stream));
+  SanityPartial host;
+  cudaError_t e = launch_sanity(D, b->state[b->cur], b->g, b->dp.G, R, parts, nb, out, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&host, out, sizeof(SanityPartial), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaFreeAsync(parts, ctx->stream);
+  cudaFreeAsync(out, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, RHYME_GPU_ECUDA, "sanity check: %s", cudaGetErrorString(e));
+  int rc = wait_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  auto cell_of = [&](long long t, int* c) {
+    c[0] = c[1] = c[2] = 0;
+    if (t < 0) return;
+    c[0] = (int)(t % b->g.n[0]) + 1;
+    const long long q = t / b->g.n[0];
+    if (D > 1) c[1] = (int)(q % b->g.n[1]) + 1;
+    if (D > 2) c[2] = (int)(q / b->g.n[1]) + 1;
+  };
+  for (int p = 0; p < SC_COUNT; ++p) {
+    rhyme_gpu_sanity_property& o = rep->prop[p];
+    o.nbelow = host.nbelow[p];
+    o.nabove = host.nabove[p];
+    o.vbelow = host.vbelow[p];
+    o.vbelow_prev = host.pbelow[p];
+    o.vabove = host.vabove[p];
+    o.vabove_prev = host.pabove[p];
+    cell_of(host.ibelow[p], o.cbelow);
+    cell_of(host.iabove[p], o.cabove);
+  }
+  for (int c = 0; c < 5; ++c) rep->nan[c] = (c < D + 2) ? host.nan[c] : 0;
+  rep->rho_min = host.rho_min;
+  rep->e_tot_min = host.e_min;
+  cell_of(host.irho_min, rep->rho_min_at);
+  cell_of(host.ie_min, rep->e_tot_min_at);
+  return RHYME_GPU_OK;
+}
+
+// ---- initial conditions painted on the device -------------------------------
+
+namespace {
+
+// Public shape -> device shape for one box: primitive vectors packed as
+// (rho, v_1..v_NDIM, p); sharp-cuboid bounds as
+// rhyme_drawing_sharp_cuboid.f90:44-53 computes them (level 0).
+int make_paint_shapes(rhyme_gpu_ctx* ctx, const Box* b, const int* le, const rhyme_gpu_shape* in, int n,
+                      std::vector<PaintShape>* out) {
+  const int D = ctx->params.ndim;
+  out->resize(n);
+  for (int i = 0; i < n; ++i) {
+    const rhyme_gpu_shape& s = in[i];
+    PaintShape& p = (*out)[i];
+    memset(&p, 0, sizeof(p));
+    if (s.type < RHYME_GPU_DRAW_CANVAS || s.type > RHYME_GPU_DRAW_SYMMETRIC_DECAYING)
+      return fail(ctx, RHYME_GPU_EINVAL, "shape %d: unknown type %d", i, s.type);
+    if (s.axis < 0 || s.axis >= D) return fail(ctx, RHYME_GPU_EINVAL, "shape %d: axis %d", i, s.axis);
+    if (s.type == RHYME_GPU_DRAW_SMOOTHED_SLAB && D < 2)
+      return fail(ctx, RHYME_GPU_EINVAL, "shape %d: a smoothed slab needs NDIM > 1", i);
+    if (s.type == RHYME_GPU_DRAW_SYMMETRIC_DECAYING && (D < 2 || !(s.sigma > 0.0)))
+      return fail(ctx, RHYME_GPU_EINVAL, "shape %d: symmetric decaying needs NDIM > 1 and sigma > 0", i);
+    if (s.type == RHYME_GPU_DRAW_HARMONIC && !(s.wavelength != 0.0))
+      return fail(ctx, RHYME_GPU_EINVAL, "shape %d: harmonic wavelength 0", i);
+    p.type = s.type;
+    p.axis = s.axis;
+    p.periodic = s.periodic ? 1 : 0;
+    p.keep_outside = s.keep_outside ? 1 : 0;
+    auto pack = [&](const double* w5, double* w) {
+      w[0] = w5[0];
+      for (int a = 0; a < D; ++a) w[1 + a] = w5[1 + a];
+      w[D + 1] = w5[4];
+    };
+    pack(s.prim[0], p.prim[0]);
+    pack(s.prim[1], p.prim[1]);
+    pack(s.base, p.base);
+    for (int a = 0; a < 3; ++a) p.origin[a] = s.origin[a];
+    p.r = s.r;
+    p.sigma = s.sigma;
+    p.pos[0] = s.pos[0];
+    p.pos[1] = s.pos[1];
+    p.slab_sigma[0] = s.slab_sigma[0];
+    p.slab_sigma[1] = s.slab_sigma[1];
+    p.amplitude = s.amplitude;
+    p.wavelength = s.wavelength;
+    p.phase = s.phase;
+    for (int a = 0; a < 3; ++a) {
+      const int dims = b->g.n[a];
+      int lb = s.left_corner[a] - le[a];
+      lb = (lb < 1) ? 1 : lb;
+      lb = (lb > dims) ? dims + 1 : lb;
+      int ub = s.left_corner[a] + s.lengths[a] - le[a];
+      ub = (ub < 1) ? 0 : ub;
+      ub = (ub > dims) ? dims : ub;
+      p.lb[a] = (a < D) ? lb : 1;
+      p.ub[a] = (a < D) ? ub : 1;
+    }
+  }
+  return RHYME_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int rhyme_gpu_paint(rhyme_gpu_ctx* ctx, int handle, const int left_edge[3], const rhyme_gpu_shape* shapes,
+                               int n) {
+  if (!ctx || !left_edge || (n > 0 && !shapes) || n < 0) return fail(ctx, RHYME_GPU_EINVAL, "bad argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  if (n == 0) return RHYME_GPU_OK;
+  std::vector<PaintShape> ps;
+  int rc = make_paint_shapes(ctx, b, left_edge, shapes, n, &ps);
+  if (rc != RHYME_GPU_OK) return rc;
+  PaintShape* d = nullptr;
+  CK(cudaMallocAsync((void**)&d, sizeof(PaintShape) * n, ctx->stream));
+  cudaError_t e = cudaMemcpyAsync(d, ps.data(), sizeof(PaintShape) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_paint(ctx->params.ndim, d, n, b->dp.G, b->g, left_edge, b->state[b->cur],
+                     ctx->mixed ? b->Uf[b->cur] : nullptr, ctx->stream);
+  cudaFreeAsync(d, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, RHYME_GPU_ECUDA, "paint: %s", cudaGetErrorString(e));
+  return RHYME_GPU_OK;
+}
+
 extern "C" int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int tile_cells[3],
                                     int tile_pencils[3]) {
   if (!ctx || !dx || !tile_cells || !tile_pencils) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
@@ -1208,6 +1477,9 @@ struct ServerReq {
   long long cells = 0;
   void* staging = nullptr;
   size_t staging_bytes = 0;
+  void* out_staging = nullptr;  // FP32 level output (r.output set)
+  size_t out_staging_bytes = 0;
+  std::vector<rhyme_gpu_shape> shapes;  // painted initial state (r.nshapes > 0)
   cudaEvent_t ev = nullptr;
 };
 
@@ -1314,8 +1586,11 @@ int rhyme_gpu_server_submit(rhyme_gpu_server* S, const rhyme_gpu_request* r, int
   for (int a = 0; a < 3; ++a)
     if ((a < r->ndim && r->dims[a] < 1) || (a >= r->ndim && r->dims[a] != 1))
       return server_fail(S, RHYME_GPU_EINVAL, "bad request dims");
+  if (r->nshapes < 0 || (r->nshapes > 0 && !r->shapes)) return server_fail(S, RHYME_GPU_EINVAL, "bad shape list");
   ServerReq q;
   q.r = *r;
+  if (r->nshapes > 0) q.shapes.assign(r->shapes, r->shapes + r->nshapes);  // kept until admission
+  q.r.shapes = nullptr;
   q.t_submit = server_now(S);
   q.bytes = box_device_bytes(r->ndim, S->ctx[0]->mixed, r->dims);
   q.cells = (long long)r->dims[0] * r->dims[1] * r->dims[2];
@@ -1342,6 +1617,11 @@ int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, in
     memcpy(q.r.cells, q.staging, (size_t)(D + 2) * g.field * sizeof(double));
     pinned_put(S, q.staging, q.staging_bytes);
     q.staging = nullptr;
+    if (q.out_staging) {
+      memcpy(q.r.output, q.out_staging, (size_t)(D + 2) * q.cells * sizeof(float));
+      pinned_put(S, q.out_staging, q.out_staging_bytes);
+      q.out_staging = nullptr;
+    }
     cudaEventDestroy(q.ev);
     q.ev = nullptr;
     q.t_done = server_now(S);
@@ -1361,10 +1641,22 @@ int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, in
     const size_t hb = (size_t)(q.r.ndim + 2) * g.field * sizeof(double);
     q.staging = pinned_get(S, hb, &q.staging_bytes);
     if (!q.staging) return server_fail(S, RHYME_GPU_ENOMEM, "pinned staging allocation failed");
-    memcpy(q.staging, q.r.cells, hb);
+    const bool painted = !q.shapes.empty();
+    if (!painted) memcpy(q.staging, q.r.cells, hb);
     int h = -1;
-    int rc = register_box_impl(ctx, 0, id, (double*)q.staging, q.r.dims, 2, q.r.ndim + 2, false, true, &h, true);
+    int rc = register_box_impl(ctx, 0, id, (double*)q.staging, q.r.dims, 2, q.r.ndim + 2, false, !painted, &h, true);
     if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+    if (painted) {  // initial state painted on the device from zero cells: no upload
+      Box* nb = ctx->boxes[h];
+      for (int i = 0; i < 2; ++i) {
+        cudaError_t e = cudaMemsetAsync(nb->state[i], 0, nb->hydro_bytes, ctx->stream);
+        if (e == cudaSuccess && nb->Uf[i]) e = cudaMemsetAsync(nb->Uf[i], 0, nb->hydro_bytes / 2, ctx->stream);
+        if (e != cudaSuccess) return server_fail(S, RHYME_GPU_ECUDA, cudaGetErrorString(e));
+      }
+      const int le[3] = {1, 1, 1};
+      rc = rhyme_gpu_paint(ctx, h, le, q.shapes.data(), (int)q.shapes.size());
+      if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
+    }
     rc = rhyme_gpu_set_box_params(ctx, h, q.r.bc, q.r.limiter, q.r.omega);
     if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
     ctx->boxes[h]->dx = make_dx(q.r.ndim, q.r.dx);
@@ -1418,6 +1710,36 @@ int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, in
       cudaStreamWaitEvent(S->copy, done_compute, 0);
       cudaEventDestroy(done_compute);
       cudaMemcpyAsync(q.staging, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, S->copy);
+      if (q.r.output) {
+        // one-box level output: packed on the compute stream, drained on the copy stream
+        const int D = q.r.ndim;
+        const size_t ob = (size_t)(D + 2) * q.cells * sizeof(float);
+        q.out_staging = pinned_get(S, ob, &q.out_staging_bytes);
+        if (!q.out_staging) return server_fail(S, RHYME_GPU_ENOMEM, "pinned staging allocation failed");
+        PackDesc pd;
+        pd.U = b->state[b->cur];
+        pd.g = b->g;
+        pd.cells = q.cells;
+        pd.hydro_off = 0;
+        pd.out_off = 0;
+        PackDesc* d_pd = nullptr;
+        float* d_out = nullptr;
+        cudaError_t e = cudaMallocAsync((void**)&d_pd, sizeof(PackDesc), ctx->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_out, ob, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_pd, &pd, sizeof(PackDesc), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = launch_pack_level(d_pd, 1, (long long)(D + 2) * q.cells, D, d_out, ctx->stream);
+        cudaEvent_t packed;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&packed, cudaEventDisableTiming);
+        if (e == cudaSuccess) {
+          cudaEventRecord(packed, ctx->stream);
+          cudaStreamWaitEvent(S->copy, packed, 0);
+          cudaEventDestroy(packed);
+          e = cudaMemcpyAsync(q.out_staging, d_out, ob, cudaMemcpyDeviceToHost, S->copy);
+        }
+        if (d_pd) cudaFreeAsync(d_pd, S->copy);
+        if (d_out) cudaFreeAsync(d_out, S->copy);
+        if (e != cudaSuccess) return server_fail(S, RHYME_GPU_ECUDA, cudaGetErrorString(e));
+      }
       cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming);
       cudaEventRecord(q.ev, S->copy);
       // the batch tables reference this box: drop the batch before freeing

@@ -21,6 +21,27 @@ constexpr int kSweepThreads = 256;
 // acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
 enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
 
+// The flux difference dt/dx (F_left - F_right) of one component of one cell
+// and its accumulation by mode, with explicit roundings (a fused
+// multiply-add onto the running sum) so that every sweep variant performs
+// exactly the same operations.
+template <int MODE>
+__device__ __forceinline__ void accumulate(float dtdx, float fl, float fr, long long oc, float* __restrict__ acc,
+                                           const double* __restrict__ U, double* __restrict__ Unew,
+                                           float* __restrict__ Ufnew) {
+  const float d = __fsub_rn(fl, fr);
+  if (MODE == FIRST) {
+    acc[oc] = __fmul_rn(dtdx, d);
+  } else if (MODE == MID) {
+    acc[oc] = __fmaf_rn(dtdx, d, acc[oc]);
+  } else {
+    const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, acc[oc]) : __fmul_rn(dtdx, d);
+    const double un = __dadd_rn(U[oc], (double)tot);
+    Unew[oc] = un;
+    Ufnew[oc] = (float)un;
+  }
+}
+
 // Slab geometry of axis A: pencils run along B (x unless A is x).
 template <int D, int A>
 struct Axes {
@@ -169,20 +190,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     if (ga > NA || gb > NB) continue;
     const long long o = offset(ga, gb);
 #pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      const float x = dtdx * (sh.f[c][ix(lu, lb, S + 1)] - sh.f[c][ix(lu + 1, lb, S + 1)]);
-      const long long oc = (long long)c * F + o;
-      if (MODE == FIRST) {
-        acc[oc] = x;
-      } else if (MODE == MID) {
-        acc[oc] = acc[oc] + x;
-      } else {
-        const float tot = (MODE == LAST) ? acc[oc] + x : x;
-        const double un = U[oc] + (double)tot;
-        Unew[oc] = un;
-        Ufnew[oc] = (float)un;
-      }
-    }
+    for (int c = 0; c < D + 2; ++c)
+      accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)], (long long)c * F + o,
+                       acc, U, Unew, Ufnew);
   }
 }
 
@@ -228,6 +238,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                                  q, w.box, tA, tB, cC, sh);
   }
 }
+
 
 }  // namespace
 }  // namespace rgpu

@@ -35,15 +35,45 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
            "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
            "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
-           "rhyme_gpu_server_destroy", "rhyme_gpu_sweep_plan"]
+           "rhyme_gpu_server_destroy", "rhyme_gpu_sweep_plan",
+           "rhyme_gpu_output_level", "rhyme_gpu_output_wait", "rhyme_gpu_box_totals",
+           "rhyme_gpu_sanity_check", "rhyme_gpu_paint"]
 REQ_PENDING, REQ_ACTIVE, REQ_DRAINING, REQ_DONE = 0, 1, 2, 3
+
+
+class Shape(C.Structure):
+    """struct rhyme_gpu_shape (include/rhyme_gpu.h); see rhyme_gb300.drawing."""
+    _fields_ = [("type", C.c_int), ("axis", C.c_int), ("periodic", C.c_int), ("keep_outside", C.c_int),
+                ("left_corner", C.c_int * 3), ("lengths", C.c_int * 3), ("prim", (C.c_double * 5) * 2),
+                ("origin", C.c_double * 3), ("r", C.c_double), ("sigma", C.c_double), ("pos", C.c_double * 2),
+                ("slab_sigma", C.c_double * 2), ("amplitude", C.c_double), ("wavelength", C.c_double),
+                ("phase", C.c_double), ("base", C.c_double * 5)]
 
 
 class Request(C.Structure):
     """struct rhyme_gpu_request (include/rhyme_gpu.h)."""
     _fields_ = [("ndim", C.c_int), ("dims", C.c_int * 3), ("nsteps", C.c_int), ("limiter", C.c_int),
                 ("bc", C.c_int * 6), ("omega", C.c_double), ("dx", C.c_double * 3),
-                ("cells", C.POINTER(C.c_double))]
+                ("cells", C.POINTER(C.c_double)), ("output", C.POINTER(C.c_float)),
+                ("shapes", C.POINTER(Shape)), ("nshapes", C.c_int), ("reserved", C.c_int)]
+SANITY_PROPERTIES = ["rho", "vx", "vy", "vz", "e_tot", "abs_v", "mach"]
+
+
+class SanityProperty(C.Structure):
+    """struct rhyme_gpu_sanity_property (include/rhyme_gpu.h)."""
+    _fields_ = [("range", C.c_double * 2), ("enabled", C.c_int), ("reserved", C.c_int),
+                ("nbelow", C.c_longlong), ("nabove", C.c_longlong), ("vbelow", C.c_double),
+                ("vbelow_prev", C.c_double), ("vabove", C.c_double), ("vabove_prev", C.c_double),
+                ("cbelow", C.c_int * 3), ("cabove", C.c_int * 3)]
+
+
+class SanityReport(C.Structure):
+    """struct rhyme_gpu_sanity_report (include/rhyme_gpu.h)."""
+    _fields_ = [("prop", SanityProperty * 7), ("nan", C.c_int * 5), ("reserved", C.c_int),
+                ("rho_min", C.c_double), ("e_tot_min", C.c_double), ("rho_min_at", C.c_int * 3),
+                ("e_tot_min_at", C.c_int * 3)]
+
+
 PHASES = ["cfl", "ghost_fill", "faces", "fluxes", "update"]
 PHASES_MIXED = ["cfl", "ghost_fill", "sweep_x", "sweep_y", "sweep_z"]
 
@@ -126,6 +156,11 @@ def load():
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     L.rhyme_gpu_sweep_plan.argtypes = [vp, C.c_int, dp, ip, ip]
+    L.rhyme_gpu_output_level.argtypes = [vp, ip, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_longlong]
+    L.rhyme_gpu_output_wait.argtypes = [vp]
+    L.rhyme_gpu_box_totals.argtypes = [vp, C.c_int, dp]
+    L.rhyme_gpu_sanity_check.argtypes = [vp, C.c_int, C.POINTER(SanityReport)]
+    L.rhyme_gpu_paint.argtypes = [vp, C.c_int, ip, C.POINTER(Shape), C.c_int]
     L.rhyme_gpu_mh_solve_noalloc.argtypes = [C.POINTER(Params), vp, vp, ip, dp, C.c_double, vp]
     L.rhyme_gpu_set_box_params.argtypes = [vp, C.c_int, ip, C.c_int, C.c_double]
     L.rhyme_gpu_batch_create.argtypes = [vp, ip, dp, C.c_int, C.POINTER(vp)]
@@ -291,6 +326,61 @@ class Context:
                                                   p.ctypes.data_as(C.POINTER(C.c_int))))
         return [(int(a), int(b)) for a, b in zip(s, p) if a]
 
+    def output_level(self, boxes, ncmp=None, out=None):
+        """Start the level output of `boxes` (the Chombo "data:datatype=0"
+        layout, FP32, hydro components); returns the float32 array that
+        receives it once output_wait() returns."""
+        ncmp = self.ndim + 2 if ncmp is None else int(ncmp)
+        n = sum(int(np.prod(b.dims[:self.ndim])) for b in boxes) * ncmp
+        if out is None:
+            out = np.zeros(n, dtype=np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous
+        handles = np.array([b.handle for b in boxes], dtype=np.int32)
+        self._keep_out = (out, handles)
+        self._check(self.lib.rhyme_gpu_output_level(self.h, handles.ctypes.data_as(C.POINTER(C.c_int)),
+                                                    len(boxes), ncmp, out.ctypes.data_as(C.POINTER(C.c_float)),
+                                                    out.size))
+        return out
+
+    def box_totals(self, box):
+        """(sum of rho > 0, sum of e_tot > 0) over all cells, ghosts included."""
+        t = np.zeros(2)
+        self._check(self.lib.rhyme_gpu_box_totals(self.h, box.handle, _d(t)))
+        return float(t[0]), float(t[1])
+
+    def sanity_check(self, box, ranges):
+        """ranges: {property: (lo, hi)} for the enabled properties (names in
+        SANITY_PROPERTIES). Returns (report dict per property, general
+        checks dict)."""
+        rep = SanityReport()
+        for i, name in enumerate(SANITY_PROPERTIES):
+            if name in ranges:
+                rep.prop[i].enabled = 1
+                rep.prop[i].range[0], rep.prop[i].range[1] = ranges[name]
+        self._check(self.lib.rhyme_gpu_sanity_check(self.h, box.handle, C.byref(rep)))
+        props = {}
+        for i, name in enumerate(SANITY_PROPERTIES):
+            if name in ranges:
+                q = rep.prop[i]
+                props[name] = dict(nbelow=q.nbelow, nabove=q.nabove, vbelow=q.vbelow, vbelow_prev=q.vbelow_prev,
+                                   vabove=q.vabove, vabove_prev=q.vabove_prev, cbelow=tuple(q.cbelow),
+                                   cabove=tuple(q.cabove))
+        general = dict(nan=[bool(x) for x in rep.nan[:self.ndim + 2]], rho_min=rep.rho_min,
+                       e_tot_min=rep.e_tot_min, rho_min_at=tuple(rep.rho_min_at),
+                       e_tot_min_at=tuple(rep.e_tot_min_at))
+        return props, general
+
+    def paint(self, box, shapes, left_edge=(1, 1, 1)):
+        """Paint the box's initial state on the device from a list of Shape
+        (rhyme_gb300.drawing builds them)."""
+        arr = (Shape * max(1, len(shapes)))(*shapes)
+        le = np.asarray(list(left_edge) + [1] * (3 - len(left_edge)), dtype=np.int32)
+        self._check(self.lib.rhyme_gpu_paint(self.h, box.handle, le.ctypes.data_as(C.POINTER(C.c_int)), arr,
+                                             len(shapes)))
+
+    def output_wait(self):
+        self._check(self.lib.rhyme_gpu_output_wait(self.h))
+
     def synchronize(self):
         self._check(self.lib.rhyme_gpu_synchronize(self.h))
 
@@ -389,8 +479,11 @@ class Server:
         if rc != OK:
             raise RhymeGpuError(rc, self.lib.rhyme_gpu_server_last_error(self.h).decode())
 
-    def submit(self, cells, nsteps, dx, limiter, bc, omega=0.0):
-        """Queue one solve; `cells` (NDIM+2, ...) receives the result."""
+    def submit(self, cells, nsteps, dx, limiter, bc, omega=0.0, output=None, shapes=None):
+        """Queue one solve; `cells` (NDIM+2, ...) receives the result and, if
+        given, `output` (float32, (NDIM+2) x interior cells) the result in the
+        Chombo level-data layout; with `shapes` (rhyme_gb300.drawing) the
+        initial state is painted on the device instead of uploaded."""
         assert cells.dtype == np.float64 and cells.flags.c_contiguous
         r = Request()
         nd = cells.ndim - 1
@@ -405,9 +498,18 @@ class Server:
             r.bc[i] = int(bc[i]) if i < len(bc) else 2
         r.omega = float(omega)
         r.cells = _d(cells)
+        if output is not None:
+            assert output.dtype == np.float32 and output.flags.c_contiguous
+            assert output.size == (nd + 2) * int(np.prod([r.dims[a] for a in range(nd)]))
+            r.output = output.ctypes.data_as(C.POINTER(C.c_float))
+        arr = None
+        if shapes:
+            arr = (Shape * len(shapes))(*shapes)
+            r.shapes = C.cast(arr, C.POINTER(Shape))
+            r.nshapes = len(shapes)
         rid = C.c_int()
         self._check(self.lib.rhyme_gpu_server_submit(self.h, C.byref(r), C.byref(rid)))
-        self._keep[rid.value] = cells
+        self._keep[rid.value] = (cells, output)
         return rid.value
 
     def tick(self):

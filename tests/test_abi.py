@@ -38,6 +38,11 @@ def test_abi_version(lib):
 def test_params_layout():
     # 10 ints (incl. bc[6]) + precision + sweep_tuning = 12 ints, then 7 doubles, then 30 doubles
     assert C.sizeof(gpu.Params) == 12 * 4 + 7 * 8 + 30 * 8
+    # struct rhyme_gpu_request: 12 ints, omega + dx[3], cells, output and
+    # shapes pointers, nshapes + reserved
+    assert C.sizeof(gpu.Request) == 12 * 4 + 4 * 8 + 3 * 8 + 2 * 4
+    # struct rhyme_gpu_shape: 4 ints, 6 ints, 10 + 3 + 2 + 2 + 2 + 3 + 5 doubles
+    assert C.sizeof(gpu.Shape) == 10 * 4 + 27 * 8
     assert gpu.Params.gamma.offset == 48
 
 

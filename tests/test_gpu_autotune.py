@@ -1,7 +1,7 @@
 """Autotuner of the mixed-precision sweeps: the chosen tile shapes come from
-the candidate set, a box-size class is tuned once per context, and the
-result of a step does not depend on the shape (each interface is solved by
-one thread from the same staged values, whatever the tiling)."""
+the candidate set, and the result of a step does not depend on the shape
+(each face state and interface is computed by one thread from the same FP32
+values with the same operations, and the accumulation rounds explicitly)."""
 import numpy as np
 import pytest
 
@@ -10,6 +10,7 @@ from rhyme_gb300.params import MIXED, OUTFLOW, PERIODIC, REFLECTIVE, hydro_param
 
 pytestmark = pytest.mark.gpu
 
+# tiles: (cells along the axis, pencils)
 CANDIDATES = {1: [(64, 1), (128, 1), (256, 1), (512, 1)],
               2: [(8, 32), (16, 16), (32, 8), (64, 4)],
               3: [(8, 32), (16, 16), (32, 8), (64, 4)]}

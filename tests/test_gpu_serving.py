@@ -81,3 +81,27 @@ def test_admission_cap():
     for r, o in zip(reqs, outs):
         ref = _alone(r, MIXED)
         assert max(e[0] for e in field_errors(o, ref, o.ndim - 1)) <= 1e-12
+
+
+def test_served_output_drain():
+    """Requests that ask for it also receive their result in the Chombo
+    level-data layout (FP32), equal to packing the FP64 result."""
+    from oracle import chombo_pack
+    reqs = _requests(9, 6)
+    base = hydro_params(3, precision=MIXED)
+    outs = [r["cells"].copy() for r in reqs]
+    levels = []
+    with gpu.Server(base, COURANT, 150 << 30, 64) as srv:
+        ids = []
+        for o, r in zip(outs, reqs):
+            nd = o.ndim - 1
+            lv = np.zeros((nd + 2) * int(np.prod([s - 4 for s in o.shape[1:]])), dtype=np.float32)
+            levels.append(lv)
+            ids.append(srv.submit(o, r["nsteps"], r["dx"], r["limiter"], r["bc"], output=lv))
+        for _ in range(10000):
+            a, p, d = srv.tick()
+            if a == 0 and p == 0 and d == 0:
+                break
+        assert all(srv.request(i)[0] == gpu.REQ_DONE for i in ids)
+    for o, lv in zip(outs, levels):
+        assert np.array_equal(lv, chombo_pack.pack_level([o]))
