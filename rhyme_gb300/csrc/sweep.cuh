@@ -1,6 +1,6 @@
 // sweep.cuh -- the fused per-axis sweep of the mixed-precision step.
 //
-// A CTA of kSweepThreads threads stages a slab of the FP32 mirror Uf (S
+// A CTA of TileCfg<S,P>::threads threads stages a slab of the FP32 mirror Uf (S
 // cells along the sweep axis plus the 2-cell ghost/halo layer, for P
 // pencils) in shared memory with coalesced loads, computes FP32 limited
 // slopes and half-step face states for S+2 cells, solves the S+1 exact
@@ -15,7 +15,16 @@
 namespace rgpu {
 namespace {
 
-constexpr int kSweepThreads = 256;
+// Threads of a tile's CTA: one per interface of the tile ((S+1)·P, the
+// costliest phase), rounded up to whole warps, so that no phase but the
+// shared-memory staging needs a second, mostly idle round behind a barrier;
+// at most 512. CTAs per SM such that a thread may keep up to 72 registers.
+template <int S, int P>
+struct TileCfg {
+  static constexpr int warps_ = ((S + 1) * P + 31) / 32;
+  static constexpr int threads = warps_ * 32 > 512 ? 512 : warps_ * 32;
+  static constexpr int min_ctas = 65536 / (threads * 72) > 0 ? 65536 / (threads * 72) : 1;
+};
 
 // Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),
 // acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
@@ -104,7 +113,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
 
   // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
-  for (int it = threadIdx.x; it < (S + 4) * P; it += kSweepThreads) {
+  for (int it = threadIdx.x; it < (S + 4) * P; it += TileCfg<S, P>::threads) {
     int la, lb;
     split(it, S + 4, la, lb);
     const int ga = a0 - 2 + la, gb = b0 + lb;
@@ -118,7 +127,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   const float hdtdx = s_dtdx[1];
 
   // 2. face states of cells a0-1 .. min(a0+S, NA+1)
-  for (int it = threadIdx.x; it < (S + 2) * P; it += kSweepThreads) {
+  for (int it = threadIdx.x; it < (S + 2) * P; it += TileCfg<S, P>::threads) {
     int la, lb;
     split(it, S + 2, la, lb);
     if (a0 - 1 + la > NA + 1 || b0 + lb > NB) continue;
@@ -139,7 +148,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   __syncthreads();
 
   // 3. FP32 Riemann problems at interfaces (a0-1+li | a0+li), li in [0, S]
-  for (int it = threadIdx.x; it < (S + 1) * P; it += kSweepThreads) {
+  for (int it = threadIdx.x; it < (S + 1) * P; it += TileCfg<S, P>::threads) {
     int li, lb;
     split(it, S + 1, li, lb);
     if (a0 - 1 + li > NA || b0 + lb > NB) continue;
@@ -183,7 +192,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   __syncthreads();
 
   // 4. flux differences of cells a0 .. a0+S-1 and the accumulation
-  for (int it = threadIdx.x; it < S * P; it += kSweepThreads) {
+  for (int it = threadIdx.x; it < S * P; it += TileCfg<S, P>::threads) {
     int lu, lb;
     split(it, S, lu, lb);
     const int ga = a0 + lu, gb = b0 + lb;
@@ -197,7 +206,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
 }
 
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(kSweepThreads, 4)
+__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
                  double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
@@ -214,7 +223,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 // The same sweep over the tiles of a batch of boxes, taken from a work queue
 // (item.chunk = the tile's linear index tA + nA * (tB + nB * (cC - 1))).
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(kSweepThreads, 4)
+__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
     batch_sweep_kernel(MixedParams M, const BoxDesc* __restrict__ TB, const WorkItem* __restrict__ items,
                        int n, int* head, FallbackQueue q) {
   constexpr int B = Axes<D, A>::B;

@@ -29,7 +29,7 @@ cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, c
   const int tA = (NA + S - 1) / S, tB = (NB + P - 1) / P;
   if ((A == 0 ? tB : tA) > 65535 || NC > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid = (A == 0) ? dim3(tA, tB, NC) : dim3(tB, tA, NC);
-  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, kSweepThreads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew,
+  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew,
                                                                              Ufnew, q);
   return cudaGetLastError();
 }
@@ -38,7 +38,7 @@ template <int D, int A, int S, int P>
 cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const WorkItem* items, int n, int* head,
                              const FallbackQueue& q, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  batch_sweep_kernel<D, A, S, P, mode_of<D, A>()><<<152 * 4, kSweepThreads, 0, st>>>(M, TB, items, n, head, q);
+  batch_sweep_kernel<D, A, S, P, mode_of<D, A>()><<<152 * TileCfg<S, P>::min_ctas, TileCfg<S, P>::threads, 0, st>>>(M, TB, items, n, head, q);
   return cudaGetLastError();
 }
 
