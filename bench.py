@@ -527,18 +527,21 @@ def run_batch(args, rank, local, world):
 
 def run_serve(args, rank, local, world):
     """A seeded Poisson stream of requests served by the continuous-batching
-    server (mixed precision, max 256 active, 150 GB budget) and the same
-    stream served one request at a time in plain FP64; p50/p99 latency
-    (submission to result in host memory) and cell-updates/s over the
-    makespan of each."""
+    server (mixed precision, max 256 active, 150 GB budget; initial states
+    uploaded, and painted on the device) and the same stream served one
+    request at a time in plain FP64; p50/p99 latency (submission to result
+    in host memory) and cell-updates/s over the makespan of each."""
     import torch
     from rhyme_gb300 import serving
     from rhyme_gb300.params import FP64, MIXED, hydro_params
     torch.cuda.set_device(local)
     stream = serving.make_stream(n=args.requests, rate=args.rate, seed=rank)
     out = {}
-    for name, prec, cap in (("continuous_mixed", MIXED, 256), ("one_at_a_time_fp64", FP64, 1)):
-        r = serving.replay(stream, hydro_params(3, precision=prec), hbm_budget=150 << 30, max_active=cap)
+    for name, prec, cap, paint in (("continuous_mixed", MIXED, 256, False),
+                                   ("continuous_mixed_painted", MIXED, 256, True),
+                                   ("one_at_a_time_fp64", FP64, 1, False)):
+        r = serving.replay(stream, hydro_params(3, precision=prec), hbm_budget=150 << 30, max_active=cap,
+                           paint=paint)
         lat = r["latencies"]
         out[name] = {"value": r["cell_updates"] / r["makespan"], "p50_s": float(np.percentile(lat, 50)),
                      "p99_s": float(np.percentile(lat, 99)), "makespan_s": r["makespan"],

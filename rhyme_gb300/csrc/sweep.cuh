@@ -23,7 +23,7 @@ template <int S, int P>
 struct TileCfg {
   static constexpr int warps_ = ((S + 1) * P + 31) / 32;
   static constexpr int threads = warps_ * 32 > 512 ? 512 : warps_ * 32;
-  static constexpr int min_ctas = 65536 / (threads * 72) > 0 ? 65536 / (threads * 72) : 1;
+  static constexpr int min_ctas = 65536 / (threads * 56) > 0 ? 65536 / (threads * 56) : 1;
 };
 
 // Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),

@@ -5,7 +5,9 @@ The stream: Poisson arrivals at `rate` per second; each request is 1-, 2- or
 [256, 128^3] split near-cubically, 50-500 steps, initial conditions drawn as
 in the 1-D Riemann and 3-D sphere workloads (a two-state Riemann problem
 along a random axis, or a canvas holding spheres with a harmonic density
-ripple), limiter and boundary types drawn per request.
+ripple), limiter and boundary types drawn per request. Each request holds
+its initial state both as an array and as the equivalent shape list for
+painting on the device.
 
 replay() feeds the stream to rhyme_gb300.gpu.Server at the arrival times
 (wall clock) and returns per-request latencies (done - submitted, on the
@@ -31,6 +33,9 @@ def _split(total, nd, rng):
 
 
 def _state(nd, dims, rng):
+    """The initial state as an array and as the equivalent device shape list
+    (rhyme_gb300.drawing) drawn from the same random numbers."""
+    from . import drawing
     g = GAMMA["monatomic"]
     shp = tuple(dims[::-1])
     if rng.uniform() < 0.5:
@@ -43,24 +48,37 @@ def _state(nd, dims, rng):
         vel = [np.zeros(shp) for _ in range(nd)]
         vel[axis] = np.where(left, u[0], u[1])
         U = ic.prim_to_cons(R, vel, P, g)
+        wl = [rho[0], 0.0, 0.0, 0.0, p[0]]
+        wr = [rho[1], 0.0, 0.0, 0.0, p[1]]
+        wl[1 + axis], wr[1 + axis] = u[0], u[1]
+        lengths = [dims[a] if a != axis else dims[axis] // 2 for a in range(nd)]
+        shapes = [drawing.canvas(wr), drawing.sharp_cuboid([1] * nd, lengths, wl)]
     else:
         R = np.ones(shp)
         vel = [np.zeros(shp) for _ in range(nd)]
         grids = np.indices(shp)[::-1] + 0.5
+        shapes = [drawing.canvas([1.0, 0.0, 0.0, 0.0, 1.0])]
         for _ in range(int(rng.integers(1, 5))):
             ctr = [rng.uniform(0, d) for d in dims]
             r = rng.uniform(0.1, 0.3) * min(dims)
             d2 = sum((grids[a] - ctr[a]) ** 2 for a in range(nd))
             m = d2 < r * r
-            R[m] = 10.0 ** rng.uniform(0.0, 2.0)
+            dens = 10.0 ** rng.uniform(0.0, 2.0)
+            R[m] = dens
             bulk = rng.uniform(-0.5, 0.5, nd)
             for a in range(nd):
                 vel[a][m] = bulk[a]
+            inside = [dens, 0.0, 0.0, 0.0, 1.0]
+            for a in range(nd):
+                inside[1 + a] = bulk[a]
+            shapes.append(drawing.sphere(list(ctr), r, inside, keep_outside=True))
         U = ic.prim_to_cons(R, vel, np.ones(shp), g)
-        U[0] = U[0] + 0.05 * np.cos(2.0 * np.pi * grids[0] / max(8.0, dims[0] / 8.0))
+        wavelength = max(8.0, dims[0] / 8.0)
+        U[0] = U[0] + 0.05 * np.cos(2.0 * np.pi * grids[0] / wavelength)
+        shapes.append(drawing.harmonic(0, 0.05, wavelength, [1.0, 0.0, 0.0, 0.0, 0.0]))
     cells = ic.empty_box(nd, dims)
     cells[ic.interior(nd, dims)] = U
-    return cells
+    return cells, shapes
 
 
 def make_stream(n=64, rate=10.0, seed=0, max_cells=128 ** 3):
@@ -72,17 +90,20 @@ def make_stream(n=64, rate=10.0, seed=0, max_cells=128 ** 3):
         nd = int(rng.integers(1, 4))
         total = float(np.exp(rng.uniform(np.log(256.0), np.log(float(max_cells)))))
         dims = _split(total, nd, rng)
-        cells = _state(nd, dims, rng)
+        cells, shapes = _state(nd, dims, rng)
         bc = [int(rng.choice([REFLECTIVE, OUTFLOW, PERIODIC])) for _ in range(2 * nd)] + [OUTFLOW] * (6 - 2 * nd)
-        out.append(dict(arrival=t, ndim=nd, dims=dims, cells=cells, nsteps=int(rng.integers(50, 501)),
+        out.append(dict(arrival=t, ndim=nd, dims=dims, cells=cells, shapes=shapes, nsteps=int(rng.integers(50, 501)),
                         dx=[1.0 / max(dims)] * nd, limiter=int(rng.integers(1, 5)), bc=bc))
     return out
 
 
-def replay(stream, base_params, courant=COURANT, hbm_budget=150 << 30, max_active=256, timeout_s=3600.0):
+def replay(stream, base_params, courant=COURANT, hbm_budget=150 << 30, max_active=256, timeout_s=3600.0,
+           paint=False):
     """Serve `stream` with submissions at the arrival times; returns a dict
-    with latencies (s), makespan (s), cell_updates and the results."""
-    outs = [r["cells"].copy() for r in stream]
+    with latencies (s), makespan (s), cell_updates and the results. With
+    paint, each request's initial state is painted on the device from its
+    shape list instead of uploaded."""
+    outs = [np.zeros_like(r["cells"]) if paint else r["cells"].copy() for r in stream]
     ids = [None] * len(stream)
     with gpu.Server(base_params, courant, hbm_budget, max_active) as srv:
         t0 = time.perf_counter()
@@ -92,7 +113,8 @@ def replay(stream, base_params, courant=COURANT, hbm_budget=150 << 30, max_activ
             now = time.perf_counter() - t0
             while nxt < len(stream) and stream[nxt]["arrival"] <= now:
                 r = stream[nxt]
-                ids[nxt] = srv.submit(outs[nxt], r["nsteps"], r["dx"], r["limiter"], r["bc"])
+                ids[nxt] = srv.submit(outs[nxt], r["nsteps"], r["dx"], r["limiter"], r["bc"],
+                                      shapes=r["shapes"] if paint else None)
                 nxt += 1
             a, p, d = srv.tick()
             peak = max(peak, a)

@@ -70,3 +70,17 @@ def test_output_level_leaves_other_components():
         assert (out[rest] == -7.0).all()
         off += ncmp * cells
     assert np.array_equal(first, out)
+
+
+def test_output_level_errors():
+    boxes = _boxes(2, 2, seed=3)
+    with gpu.Context(hydro_params(2)) as ctx:
+        hs = [ctx.register_box(c) for c in boxes]
+        n = sum(int(np.prod(h.dims)) for h in hs) * 4
+        with pytest.raises(gpu.RhymeGpuError) as e:
+            ctx.output_level(hs, out=np.zeros(n - 1, dtype=np.float32))
+        assert e.value.code == gpu.EINVAL
+        with pytest.raises(gpu.RhymeGpuError) as e:
+            ctx.output_level(hs, ncmp=3)
+        assert e.value.code == gpu.EINVAL
+        ctx.output_wait()  # nothing pending: returns at once

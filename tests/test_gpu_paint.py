@@ -130,3 +130,17 @@ def test_server_painted_requests():
                 break
     for x, y in zip(painted, uploaded):
         assert np.array_equal(x[:, 2:-2, 2:-2, 2:-2], y[:, 2:-2, 2:-2, 2:-2])
+
+
+def test_paint_errors():
+    with gpu.Context(hydro_params(1)) as ctx:
+        b = ctx.register_box(ic.empty_box(1, [16]))
+        bad_axis = drawing.harmonic(1, 0.1, 8.0, [1.0, 0, 0, 0, 0])
+        with pytest.raises(gpu.RhymeGpuError) as e:
+            ctx.paint(b, [bad_axis])
+        assert e.value.code == gpu.EINVAL
+        slab = drawing.smoothed_slab(0, [2.0, 8.0], [1.0, 1.0], [1.0, 0, 0, 0, 1.0], [2.0, 0, 0, 0, 1.0])
+        with pytest.raises(gpu.RhymeGpuError) as e:
+            ctx.paint(b, [slab])  # a slab needs NDIM > 1
+        assert e.value.code == gpu.EINVAL
+        ctx.paint(b, [])  # nothing to paint

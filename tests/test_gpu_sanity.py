@@ -84,3 +84,12 @@ def test_totals_after_steps():
     _, exact = osan.totals(cells)
     assert m == exact[0] or abs(m - exact[0]) <= 2 * math.ulp(exact[0])
     assert e == exact[1] or abs(e - exact[1]) <= 2 * math.ulp(exact[1])
+
+
+def test_sanity_unknown_box():
+    with gpu.Context(hydro_params(2)) as ctx:
+        b = ctx.register_box(ic.empty_box(2, [4, 4]))
+        ctx.unregister_box(b)
+        with pytest.raises(gpu.RhymeGpuError) as e:
+            ctx.box_totals(b)
+        assert e.value.code == gpu.ENOTFOUND
