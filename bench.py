@@ -546,6 +546,13 @@ def run_serve(args, rank, local, world):
         out[name] = {"value": r["cell_updates"] / r["makespan"], "p50_s": float(np.percentile(lat, 50)),
                      "p99_s": float(np.percentile(lat, 99)), "makespan_s": r["makespan"],
                      "cell_updates": r["cell_updates"], "peak_active": r["peak_active"]}
+    # capacity: the same requests all submitted at once (painted on the device)
+    burst = [dict(q, arrival=0.0) for q in stream]
+    r = serving.replay(burst, hydro_params(3, precision=MIXED), hbm_budget=150 << 30, max_active=256, paint=True)
+    out["capacity_mixed_all_at_once"] = {"value": r["cell_updates"] / r["makespan"], "makespan_s": r["makespan"],
+                                         "p50_s": float(np.percentile(r["latencies"], 50)),
+                                         "p99_s": float(np.percentile(r["latencies"], 99)),
+                                         "peak_active": r["peak_active"]}
     h = out["continuous_mixed"]
     value = allsum(h["value"], world)
     if rank == 0:

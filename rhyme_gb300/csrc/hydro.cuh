@@ -29,14 +29,19 @@ namespace rgpu {
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double m_pow(double x, double y) { return detmath::det_pow(x, y); }
-__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
-// x**y1 and x**y2 of one base (one logarithm for doubles).
+// Float powers as 2^(y log2 x) with CUDA's log2f and exp2f: the rounding of
+// the product adds a relative error of about 2^-24 |y log2 x| to the result
+// (for the positive bases of this path), against powf's ~1 ulp, for a
+// fraction of its instructions; two powers of one base share the logarithm.
+__device__ __forceinline__ float m_pow(float x, float y) { return exp2f(y * log2f(x)); }
+// x**y1 and x**y2 of one base (one logarithm).
 __device__ __forceinline__ void m_pow2(double x, double y1, double y2, double& r1, double& r2) {
   detmath::det_pow2(x, y1, y2, &r1, &r2);
 }
 __device__ __forceinline__ void m_pow2(float x, float y1, float y2, float& r1, float& r2) {
-  r1 = powf(x, y1);
-  r2 = powf(x, y2);
+  const float l = log2f(x);
+  r1 = exp2f(y1 * l);
+  r2 = exp2f(y2 * l);
 }
 __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
@@ -230,6 +235,14 @@ __device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, const WaveSide<T
     const T factor = m_sqrt(w.Ak / bp);
     f = (p - w.p) * factor;
     fprime = factor * (T(1) - (p - w.p) / (T(2) * bp));
+  } else if constexpr (sizeof(T) == sizeof(float)) {
+    // (p/p_k)^e - 1 as expm1(e log1p((p - p_k)/p_k)): the same quantity
+    // without the cancellation of the literal form when p is close to p_k
+    // (a float power near 1 carries an ulp of 1, a large relative error of
+    // the difference); p - p_k is exact there.
+    const float t = log1pf((p - w.p) / w.p);
+    f = w.c2g * expm1f(G.gm1_2g * t);
+    fprime = w.irc * expf(-G.gp1_2g * t);
   } else {
     T y, z;
     m_pow2(p / w.p, G.gm1_2g, -G.gp1_2g, y, z);
