@@ -24,14 +24,18 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (object name, source, extra flags). The plain FP64 units are compiled
 # without FMA contraction (--fmad=false) so that their arithmetic matches the
 # CPU oracle operation for operation; the mixed-precision units keep it.
+# The FP32 sweeps of the mixed form use the hardware's approximate FP32
+# division and square root (<= 2 ulp) instead of the IEEE-exact sequences.
+FP32_SWEEP_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
+
 UNITS = [
     ("kernels_box", "kernels_box.cu", ["--fmad=false"]),
     ("kernels_elem", "kernels_elem.cu", ["--fmad=false"]),
     ("rhyme_gpu", "rhyme_gpu.cu", ["--fmad=false"]),
     ("kernels_mixed", "kernels_mixed.cu", []),
-    ("sweeps_1d", "sweeps.cu", ["-DSWEEP_D=1"]),
-    ("sweeps_2d", "sweeps.cu", ["-DSWEEP_D=2"]),
-    ("sweeps_3d", "sweeps.cu", ["-DSWEEP_D=3"]),
+    ("sweeps_1d", "sweeps.cu", ["-DSWEEP_D=1"] + FP32_SWEEP_FLAGS),
+    ("sweeps_2d", "sweeps.cu", ["-DSWEEP_D=2"] + FP32_SWEEP_FLAGS),
+    ("sweeps_3d", "sweeps.cu", ["-DSWEEP_D=3"] + FP32_SWEEP_FLAGS),
     ("noalloc", "noalloc.cu", ["--fmad=false"]),
     ("kernels_batch", "kernels_batch.cu", ["--fmad=false"]),
     ("kernels_output", "kernels_output.cu", []),
