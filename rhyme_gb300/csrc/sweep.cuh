@@ -167,11 +167,20 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
         if (!isfinite(f[c])) need64 = true;
     }
     if (need64) {
-      // zero here; the FP64 correction is applied after the last sweep.
-      // Each interface is queued once: by the tile whose left face it is,
-      // or by the last tile for the box's right boundary.
+      // A non-finite cell in the interface's stencil (staged cells li .. li+3)
+      // is non-finite in FP64 too, and the FP64 redo would give NaN: give it
+      // here and queue nothing (a box the scheme has lost would otherwise
+      // queue all its interfaces every step).
+      bool finite = true;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < D + 2; ++c) finite = finite && isfinite(sh.u[c][ix(li + k, lb, S + 4)]);
+      // otherwise zero here; the FP64 correction is applied after the last
+      // sweep. Each interface is queued once: by the tile whose left face it
+      // is, or by the last tile for the box's right boundary.
       const int ga = a0 - 1 + li;
-      if (li < S || ga == NA) {
+      if (finite && (li < S || ga == NA)) {
         const int slot = atomicAdd(q.n, 1);
         if (slot < q.cap) {
           FallbackEntry& e = q.e[slot];
@@ -184,7 +193,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
         }
       }
 #pragma unroll
-      for (int c = 0; c < D + 2; ++c) f[c] = 0.f;
+      for (int c = 0; c < D + 2; ++c) f[c] = finite ? 0.f : __int_as_float(0x7fffffff);
     }
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) sh.f[c][ix(li, lb, S + 1)] = f[c];
