@@ -24,15 +24,16 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (object name, source, extra flags). The plain FP64 units are compiled
 # without FMA contraction (--fmad=false) so that their arithmetic matches the
 # CPU oracle operation for operation; the mixed-precision units keep it.
-# The FP32 sweeps of the mixed form use the hardware's approximate FP32
-# division and square root (<= 2 ulp) instead of the IEEE-exact sequences.
+# The FP32 arithmetic of the mixed form (sweeps, CFL) uses the hardware's
+# approximate FP32 division and square root (<= 2 ulp) instead of the
+# IEEE-exact sequences; FP64 arithmetic is unaffected by these flags.
 FP32_SWEEP_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
 
 UNITS = [
     ("kernels_box", "kernels_box.cu", ["--fmad=false"]),
     ("kernels_elem", "kernels_elem.cu", ["--fmad=false"]),
     ("rhyme_gpu", "rhyme_gpu.cu", ["--fmad=false"]),
-    ("kernels_mixed", "kernels_mixed.cu", []),
+    ("kernels_mixed", "kernels_mixed.cu", FP32_SWEEP_FLAGS),
     ("sweeps_1d", "sweeps.cu", ["-DSWEEP_D=1"] + FP32_SWEEP_FLAGS),
     ("sweeps_2d", "sweeps.cu", ["-DSWEEP_D=2"] + FP32_SWEEP_FLAGS),
     ("sweeps_3d", "sweeps.cu", ["-DSWEEP_D=3"] + FP32_SWEEP_FLAGS),
