@@ -1,15 +1,17 @@
 // kernels_mixed.cu -- mixed-precision MUSCL-Hancock step.
 //
 // The conserved state stays FP64 in HBM (U) and is mirrored once per step as
-// FP32 (Uf). Each axis is one fused sweep kernel: a CTA stages a slab of
-// Uf (S cells along the sweep axis plus the 2-cell ghost/halo layer, for P
-// pencils) in shared memory with coalesced loads, computes FP32 limited
-// slopes and half-step face states for S+2 cells, solves the S+1 exact
-// Riemann problems of the slab in FP32 and forms the flux difference of its
-// S cells. The flux differences of the axes are summed in FP32 in the
-// reference's association ((X + Y) + Z), and the last sweep adds the sum to
-// U in FP64 and writes U^{n+1} and its FP32 mirror: one FP64 add per
-// conserved component and cell, since on GB300 even FP64 adds are scarce.
+// FP32 (Uf) by the step's first pass, the FP32 CFL, which reads U anyway.
+// Each axis is one fused sweep kernel: a CTA stages a slab of Uf (S cells
+// along the sweep axis plus the 2-cell ghost/halo layer, for P pencils) in
+// shared memory with coalesced loads, computes FP32 limited slopes and
+// half-step face states for S+2 cells, solves the S+1 exact Riemann problems
+// of the slab in FP32 and forms the flux difference of its S cells. The flux
+// differences of the axes are summed in FP32 in the reference's association
+// ((X + Y) + Z), and the last sweep adds the sum to U in FP64 and writes
+// U^{n+1}: one FP64 add per conserved component and cell, since on GB300 even
+// FP64 adds are scarce (the next step's CFL makes the new mirror, where the
+// conversions cost nothing but bandwidth).
 //
 // Interfaces that near vacuum, or whose FP32 Newton iteration misses the
 // tolerance on its first guess, or whose FP32 face states or flux are not
@@ -18,13 +20,12 @@
 // each queued interface in FP64 from U^n, which the step leaves intact
 // (limited slopes and half-step face states of its two cells, exact Riemann
 // problem, flux: the device code of the plain path instantiated for double),
-// and applies -+ dt/dx * F to the two adjacent interior cells of U^{n+1}; a
-// second one refreshes their FP32 mirror. Keeping the FP64 code out of the
-// sweeps keeps them at ~64 registers (it tripled their register count
-// inline).
+// and applies -+ dt/dx * F to the two adjacent interior cells of U^{n+1}.
+// Keeping the FP64 code out of the sweeps keeps them at ~64 registers (it
+// tripled their register count inline).
 //
-// The CFL maximum of the mixed path is taken in FP32 over Uf; dt itself is
-// formed in FP64.
+// The CFL maximum of the mixed path is taken in FP32 over the mirror; dt
+// itself is formed in FP64.
 #include <math_constants.h>
 
 #include "rgpu_internal.h"
@@ -51,11 +52,11 @@ __global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restri
     Uf[t] = (float)U[t];
 }
 
-// |v| + cs of interior cell t of Uf in FP32; bad marks non-positive density
-// or a non-finite value.
+// Interior cell t: its FP32 mirror, written to Uf from U, and its |v| + cs in
+// FP32; bad marks non-positive density or a non-finite value.
 template <int D>
-__device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const float* __restrict__ Uf,
-                                                  const Geom& g, long long t, int& bad) {
+__device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const double* __restrict__ U,
+                                                  float* __restrict__ Uf, const Geom& g, long long t, int& bad) {
   const long long n0 = g.n[0], n1 = g.n[1];
   const int i = (int)(t % n0) + 1;
   const long long q = t / n0;
@@ -64,7 +65,10 @@ __device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const fl
   const long long o = g.at(D, i, j, k);
   float u[D + 2];
 #pragma unroll
-  for (int c = 0; c < D + 2; ++c) u[c] = Uf[(long long)c * g.field + o];
+  for (int c = 0; c < D + 2; ++c) {
+    u[c] = (float)U[(long long)c * g.field + o];
+    Uf[(long long)c * g.field + o] = u[c];
+  }
   float ss = 0.f;
 #pragma unroll
   for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
@@ -73,18 +77,19 @@ __device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const fl
   return v;
 }
 
-// FP32 signal-speed maximum over the interior of Uf; the last block forms
-// dt = courant * min(dx) / max in FP64 and resets the accumulators.
+// FP32 mirror of the interior of U and its signal-speed maximum; the last
+// block forms dt = courant * min(dx) / max in FP64 and resets the
+// accumulators.
 template <int D>
 __global__ void __launch_bounds__(kThreads)
-    cfl_f32_kernel(MixedParams M, const float* __restrict__ Uf, Geom g, double courant, double mdx,
-                   StepScratch s) {
+    cfl_f32_kernel(MixedParams M, const double* __restrict__ U, float* __restrict__ Uf, Geom g, double courant,
+                   double mdx, StepScratch s) {
   const long long total = (long long)g.n[0] * g.n[1] * (long long)g.n[2];
   float m = 0.f;
   int bad = 0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const float v = signal_speed_f32<D>(M, Uf, g, t, bad);
+    const float v = signal_speed_f32<D>(M, U, Uf, g, t, bad);
     if (v > m) m = v;
   }
 #pragma unroll
@@ -206,32 +211,10 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// FP32 mirror of the cells the fix-up touched.
-template <int D>
-__global__ void __launch_bounds__(256)
-    fallback_refresh_kernel(FallbackQueue q, Geom g, const double* __restrict__ Unew,
-                            float* __restrict__ Ufnew) {
-  const int n = min(*q.n, q.cap);
-  const long long F = g.field;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const FallbackEntry e = q.e[i];
-    const long long sa = g.s[e.axis];
-    const int NA = g.n[e.axis];
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      const long long oc = (long long)c * F + e.o;
-      if (e.ga >= 1) Ufnew[oc] = (float)Unew[oc];
-      if (e.ga + 1 <= NA) Ufnew[oc + sa] = (float)Unew[oc + sa];
-    }
-  }
-}
-
 template <int D>
 cudaError_t launch_fallback(const MixedParams& M, const FallbackQueue& q, const Geom& g, const Dx& dx,
-                            const double* dtp, const double* U, double* Unew, float* Ufnew,
-                            cudaStream_t st) {
+                            const double* dtp, const double* U, double* Unew, cudaStream_t st) {
   fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, g, dx, dtp, U, Unew);
-  fallback_refresh_kernel<D><<<152, 256, 0, st>>>(q, g, Unew, Ufnew);
   return cudaGetLastError();
 }
 
@@ -257,7 +240,7 @@ __global__ void __launch_bounds__(256)
     float m = 0.f;
     int bad = 0;
     if (t < total) {
-      const float v = signal_speed_f32<D>(M, b.Uf, b.g, t, bad);
+      const float v = signal_speed_f32<D>(M, b.U, b.Uf, b.g, t, bad);
       if (v > m) m = v;
     }
 #pragma unroll
@@ -319,29 +302,9 @@ __global__ void __launch_bounds__(128)
 }
 
 template <int D>
-__global__ void __launch_bounds__(256)
-    batch_fallback_refresh_kernel(FallbackQueue q, const BoxDesc* __restrict__ TB) {
-  const int n = min(*q.n, q.cap);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const FallbackEntry e = q.e[i];
-    const BoxDesc& b = TB[e.box];
-    const long long sa = b.g.s[e.axis];
-    const int NA = b.g.n[e.axis];
-    const long long F = b.g.field;
-#pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      const long long oc = (long long)c * F + e.o;
-      if (e.ga >= 1) b.Vf[oc] = (float)b.V[oc];
-      if (e.ga + 1 <= NA) b.Vf[oc + sa] = (float)b.V[oc + sa];
-    }
-  }
-}
-
-template <int D>
 cudaError_t launch_batch_fallback(const MixedParams& M, const BoxDesc* TB, const FallbackQueue& q,
                                   cudaStream_t st) {
   batch_fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, TB);
-  batch_fallback_refresh_kernel<D><<<152, 256, 0, st>>>(q, TB);
   return cudaGetLastError();
 }
 
@@ -352,22 +315,22 @@ cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t 
   return cudaGetLastError();
 }
 
-cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& g, double courant,
+cudaError_t launch_cfl_mixed(const MixedParams& M, const double* U, float* Uf, const Geom& g, double courant,
                              const Dx& dx, const StepScratch& s, cudaStream_t st) {
   const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
   int grid = grid_for(total, kThreads);
   if (grid > 152 * 4) grid = 152 * 4;
   switch (M.ndim) {
-    case 1: cfl_f32_kernel<1><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
-    case 2: cfl_f32_kernel<2><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
-    case 3: cfl_f32_kernel<3><<<grid, kThreads, 0, st>>>(M, Uf, g, courant, dx.min, s); break;
+    case 1: cfl_f32_kernel<1><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s); break;
+    case 2: cfl_f32_kernel<2><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s); break;
+    case 3: cfl_f32_kernel<3><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
-                                  double* Unew, float* Ufnew, float* acc, const Geom& g,
+                                  double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev) {
   // ev (optional, 3 events): recorded after the x sweep, after the y sweep
@@ -378,16 +341,16 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
   cudaError_t e = cudaMemsetAsync(q.n, 0, sizeof(int), st);
   for (int a = 0; a < D; ++a) {
     if (e == cudaSuccess)
-      e = launch_sweep_axis(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, Ufnew, q, st);
+      e = launch_sweep_axis(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, q, st);
     if (e == cudaSuccess && ev && a < 2) e = cudaEventRecord(ev[a], st);
   }
   for (int a = D; a < 2; ++a)
     if (e == cudaSuccess && ev) e = cudaEventRecord(ev[a], st);
   if (e == cudaSuccess) {
     switch (D) {
-      case 1: e = launch_fallback<1>(M, q, g, dx, s.dt, U, Unew, Ufnew, st); break;
-      case 2: e = launch_fallback<2>(M, q, g, dx, s.dt, U, Unew, Ufnew, st); break;
-      case 3: e = launch_fallback<3>(M, q, g, dx, s.dt, U, Unew, Ufnew, st); break;
+      case 1: e = launch_fallback<1>(M, q, g, dx, s.dt, U, Unew, st); break;
+      case 2: e = launch_fallback<2>(M, q, g, dx, s.dt, U, Unew, st); break;
+      case 3: e = launch_fallback<3>(M, q, g, dx, s.dt, U, Unew, st); break;
     }
   }
   if (e == cudaSuccess && ev) e = cudaEventRecord(ev[2], st);

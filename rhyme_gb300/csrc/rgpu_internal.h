@@ -146,22 +146,24 @@ int max_cfl_blocks();
 
 // Mixed-precision launchers (kernels_mixed.cu).
 cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st);
-cudaError_t launch_cfl_mixed(const MixedParams& M, const float* Uf, const Geom& g, double courant,
+// FP32 CFL of the mixed form: also writes the interior of the FP32 mirror Uf
+// from U (the sweeps read the mirror; the step that wrote U left it stale).
+cudaError_t launch_cfl_mixed(const MixedParams& M, const double* U, float* Uf, const Geom& g, double courant,
                              const Dx& dx, const StepScratch& s, cudaStream_t st);
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
-                                  double* Unew, float* Ufnew, float* acc, const Geom& g,
+                                  double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 
 // ---- batches of boxes (kernels_batch.cu) ---------------------------------
 // One entry of a batch's device box table, for one step parity: U is read,
-// V written (and the FP32 mirrors Uf / Vf in mixed precision).
+// V written (and in mixed precision the FP32 mirror Uf of U, which the
+// step's CFL pass writes).
 struct BoxDesc {
   double* U;
   double* V;
   float* Uf;
-  float* Vf;
   float* acc;
   double* faces;
   double* fluxes;
@@ -205,7 +207,7 @@ long long sweep_tile_count(int ndim, int axis, int shape, const int* n);
 #define RGPU_SWEEP_DECL(D)                                                                              \
   cudaError_t launch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const float* Uf,         \
                                     const double* U, const Geom& g, const Dx& dx, const double* dtp,    \
-                                    float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,     \
+                                    float* acc, double* Unew, const FallbackQueue& q,                   \
                                     cudaStream_t st);                                                   \
   cudaError_t launch_batch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const BoxDesc* TB, \
                                           const WorkItem* items, int n, int* head, const FallbackQueue& q, \
@@ -217,12 +219,11 @@ RGPU_SWEEP_DECL(3)
 
 inline cudaError_t launch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
                                      const double* U, const Geom& g, const Dx& dx, const double* dtp,
-                                     float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,
-                                     cudaStream_t st) {
+                                     float* acc, double* Unew, const FallbackQueue& q, cudaStream_t st) {
   switch (ndim) {
-    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -520,7 +520,7 @@ int tune_axis(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx, int axis, int* best) {
   const int c = b->cur;
   StepScratch sc = scratch_of(b, false);
   *best = default_sweep_shape(D, axis, b->g.n[axis]);
-  CK(launch_cfl_mixed(b->mp, b->Uf[c], b->g, b->dp.courant, dx, sc, ctx->stream));
+  CK(launch_cfl_mixed(b->mp, b->state[c], b->Uf[c], b->g, b->dp.courant, dx, sc, ctx->stream));
   CK(launch_ghost_fill_f32(b->dp, b->Uf[c], b->g, ctx->stream));
   cudaEvent_t ev[2];
   CK(cudaEventCreate(&ev[0]));
@@ -539,7 +539,7 @@ int tune_axis(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx, int axis, int* best) {
       if (e == cudaSuccess) e = cudaEventRecord(ev[0], ctx->stream);
       if (e == cudaSuccess)
         e = launch_sweep_axis(D, axis, k, b->mp, b->Uf[c], b->state[c], b->g, dx, sc.dt, b->acc,
-                              b->state[1 - c], b->Uf[1 - c], b->fbq, ctx->stream);
+                              b->state[1 - c], b->fbq, ctx->stream);
       if (e == cudaErrorInvalidConfiguration) {  // grid too large for this shape
         ok = false;
         break;
@@ -596,11 +596,11 @@ cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool
   double* U = b->state[cur];
   double* V = b->state[1 - cur];
   if (ctx->mixed) {
-    cudaError_t e = launch_cfl_mixed(b->mp, b->Uf[cur], b->g, b->dp.courant, dx, s, ctx->stream);
+    cudaError_t e = launch_cfl_mixed(b->mp, U, b->Uf[cur], b->g, b->dp.courant, dx, s, ctx->stream);
     if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
     if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[cur], b->g, ctx->stream);
     if (e == cudaSuccess)
-      e = launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->Uf[1 - cur], b->acc, b->g, dx, s, b->fbq,
+      e = launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->acc, b->g, dx, s, b->fbq,
                                 b->plan, ctx->stream);
     return e;
   }
@@ -649,7 +649,8 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], 
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   Dx d = make_dx(ctx->params.ndim, dx);
   if (ctx->mixed)
-    CK(launch_cfl_mixed(b->mp, b->Uf[b->cur], b->g, b->dp.courant, d, scratch_of(b, false), ctx->stream));
+    CK(launch_cfl_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->g, b->dp.courant, d, scratch_of(b, false),
+                        ctx->stream));
   else
     CK(launch_cfl(b->dp, b->state[b->cur], b->g, d, scratch_of(b, false), ctx->stream));
   CK(cudaMemcpyAsync(ctx->pinned_dt, b->s.dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -688,9 +689,14 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   if (rc != RHYME_GPU_OK) return rc;
   ctx->pinned_dt[0] = dt;
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  if (ctx->mixed)
-    CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->Uf[1 - b->cur],
-                             b->acc, b->g, d, scratch_of(b, false), b->fbq, b->plan, ctx->stream));
+  if (ctx->mixed) {
+    // the FP32 mirror of the whole box (ghosts included) from the state this
+    // solve reads: a driver may call the solve without the CFL pass that
+    // otherwise writes the mirror
+    CK(launch_to_f32(b->state[b->cur], b->Uf[b->cur], (long long)(ctx->params.ndim + 2) * b->g.field, ctx->stream));
+    CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->acc, b->g, d,
+                             scratch_of(b, false), b->fbq, b->plan, ctx->stream));
+  }
   else
     CK(launch_mh_solve(b->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
                        ctx->stream));
@@ -858,13 +864,13 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
     if (ctx->mixed) {
       // mixed: ms[2..4] are the x, y and z sweeps (the last one with the
       // FP64 fix-up of the queued interfaces)
-      if (e == cudaSuccess) e = launch_cfl_mixed(b->mp, b->Uf[b->cur], b->g, b->dp.courant, d, sc, ctx->stream);
+      if (e == cudaSuccess) e = launch_cfl_mixed(b->mp, U, b->Uf[b->cur], b->g, b->dp.courant, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
       if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream);
       if (e == cudaSuccess) e = launch_ghost_fill_f32(b->dp, b->Uf[b->cur], b->g, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
       if (e == cudaSuccess)
-        e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->Uf[1 - b->cur], b->acc, b->g, d, sc,
+        e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->acc, b->g, d, sc,
                                   b->fbq, b->plan, ctx->stream, ev + 3);
     } else {
       if (e == cudaSuccess) e = launch_cfl(b->dp, U, b->g, d, sc, ctx->stream);
@@ -1266,7 +1272,6 @@ int batch_build(rhyme_gpu_batch* B) {
       d.U = b->state[c];
       d.V = b->state[1 - c];
       d.Uf = b->Uf[c];
-      d.Vf = b->Uf[1 - c];
       d.acc = b->acc;
       d.faces = b->s.faces;
       d.fluxes = b->s.fluxes;

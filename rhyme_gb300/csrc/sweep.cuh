@@ -36,8 +36,7 @@ enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
 // exactly the same operations.
 template <int MODE>
 __device__ __forceinline__ void accumulate(float dtdx, float fl, float fr, long long oc, float* __restrict__ acc,
-                                           const double* __restrict__ U, double* __restrict__ Unew,
-                                           float* __restrict__ Ufnew) {
+                                           const double* __restrict__ U, double* __restrict__ Unew) {
   const float d = __fsub_rn(fl, fr);
   if (MODE == FIRST) {
     acc[oc] = __fmul_rn(dtdx, d);
@@ -45,9 +44,7 @@ __device__ __forceinline__ void accumulate(float dtdx, float fl, float fr, long 
     acc[oc] = __fmaf_rn(dtdx, d, acc[oc]);
   } else {
     const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, acc[oc]) : __fmul_rn(dtdx, d);
-    const double un = __dadd_rn(U[oc], (double)tot);
-    Unew[oc] = un;
-    Ufnew[oc] = (float)un;
+    Unew[oc] = __dadd_rn(U[oc], (double)tot);
   }
 }
 
@@ -76,7 +73,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
                                            const float* __restrict__ Uf, const double* __restrict__ U,
                                            const Geom& g, const Dx& dx, const double* __restrict__ dtp,
                                            float* __restrict__ acc, double* __restrict__ Unew,
-                                           float* __restrict__ Ufnew, const FallbackQueue& q, int box,
+                                           const FallbackQueue& q, int box,
                                            int tA, int tB, int cC, SweepSmem<D, S, P>& sh) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   const int NA = g.n[A];
@@ -210,7 +207,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
       accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)], (long long)c * F + o,
-                       acc, U, Unew, Ufnew);
+                       acc, U, Unew);
   }
 }
 
@@ -218,14 +215,14 @@ template <int D, int A, int S, int P, int MODE>
 __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
-                 double* __restrict__ Unew, float* __restrict__ Ufnew, FallbackQueue q) {
+                 double* __restrict__ Unew, FallbackQueue q) {
   constexpr int C = Axes<D, A>::C;
   __shared__ SweepSmem<D, S, P> sh;
   // tile origin: the fast grid axis runs along x
   const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
   const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
   const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
-  sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, 0, tA, tB, cC,
+  sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, q, 0, tA, tB, cC,
                                sh);
 }
 
@@ -252,7 +249,7 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
     const long long r = w.chunk / nA;
     const int tB = (int)(r % nB);
     const int cC = (int)(r / nB) + 1;
-    sweep_tile<D, A, S, P, MODE>(M, b.limiter, b.omega_f, b.Uf, b.U, b.g, b.dx, b.ctl, b.acc, b.V, b.Vf,
+    sweep_tile<D, A, S, P, MODE>(M, b.limiter, b.omega_f, b.Uf, b.U, b.g, b.dx, b.ctl, b.acc, b.V,
                                  q, w.box, tA, tB, cC, sh);
   }
 }

@@ -20,7 +20,7 @@ constexpr int mode_of() {
 
 template <int D, int A, int S, int P>
 cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, const Geom& g, const Dx& dx,
-                       const double* dtp, float* acc, double* Unew, float* Ufnew, const FallbackQueue& q,
+                       const double* dtp, float* acc, double* Unew, const FallbackQueue& q,
                        cudaStream_t st) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   const int NA = g.n[A];
@@ -29,8 +29,7 @@ cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, c
   const int tA = (NA + S - 1) / S, tB = (NB + P - 1) / P;
   if ((A == 0 ? tB : tA) > 65535 || NC > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid = (A == 0) ? dim3(tA, tB, NC) : dim3(tB, tA, NC);
-  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew,
-                                                                             Ufnew, q);
+  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew, q);
   return cudaGetLastError();
 }
 
@@ -45,21 +44,21 @@ cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const Work
 // shape index -> (S, P) as in sweep_shape()
 template <int D, int A>
 cudaError_t by_shape(int shape, const MixedParams& M, const float* Uf, const double* U, const Geom& g,
-                     const Dx& dx, const double* dtp, float* acc, double* Unew, float* Ufnew,
+                     const Dx& dx, const double* dtp, float* acc, double* Unew,
                      const FallbackQueue& q, cudaStream_t st) {
   if constexpr (D == 1) {
     switch (shape) {
-      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
     }
   } else {
     switch (shape) {
-      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
-      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
     }
   }
   return cudaErrorInvalidValue;
@@ -93,16 +92,16 @@ cudaError_t batch_by_shape(int shape, const MixedParams& M, const BoxDesc* TB, c
 
 cudaError_t RGPU_CAT(launch_sweep_axis_, SWEEP_D)(int axis, int shape, const MixedParams& M, const float* Uf,
                                                  const double* U, const Geom& g, const Dx& dx,
-                                                 const double* dtp, float* acc, double* Unew, float* Ufnew,
+                                                 const double* dtp, float* acc, double* Unew,
                                                  const FallbackQueue& q, cudaStream_t st) {
   constexpr int D = SWEEP_D;
   switch (axis) {
-    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
     case 1:
-      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
       break;
     case 2:
-      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, Ufnew, q, st);
+      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
       break;
   }
   return cudaErrorInvalidValue;
