@@ -126,11 +126,32 @@ int rhyme_gpu_register_box(rhyme_gpu_ctx* ctx, int level, int number,
                            int ncmp, int* handle);
 int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle);
 
-/* Host -> device copy of the hydro components (and ghosts) of a box. */
+/* Host -> device copy of the hydro components (and ghosts) of a box.
+ * Asynchronous: the array the library page-locked at registration must
+ * not be written until a later call waits on the context stream (every
+ * call that returns a value does). For a 2-D or 3-D box in mixed precision
+ * of 16 MiB or more the copy runs in slabs of rows of the outermost axis,
+ * each slab's share of the CFL maximum taken while the next one is in
+ * flight, and the next rhyme_gpu_cfl_time_step only forms dt from it. */
 int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle);
 /* Device -> host copy into the registered cells array; waits for the stream
- * (bounded wait, RHYME_GPU_ETIMEDOUT). */
+ * (bounded wait, RHYME_GPU_ETIMEDOUT). With host write-back on, the last
+ * solve's copies are already in flight and this only waits for them. */
 int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle);
+
+/*
+ * Host write-back (default off). With on != 0 every rhyme_gpu_mh_solve of
+ * the box also copies the new state into the registered cells array: the
+ * drop-in mode, in which the shim's rhyme_muscl_hancock_solve returns with
+ * box%cells current (the reference updates box%cells in place,
+ * rhyme_muscl_hancock_solve_memory_intensive.f90:148-179), for the host
+ * readers of src/main.f90:122-155. For a box whose upload runs in slabs
+ * (rhyme_gpu_sync_to_device) the solve runs in slabs of rows as well and
+ * each slab's finished rows are copied while the next slab is solved;
+ * otherwise one copy follows the solve. The array is being written until
+ * rhyme_gpu_sync_to_host or rhyme_gpu_synchronize returns.
+ */
+int rhyme_gpu_set_host_writeback(rhyme_gpu_ctx* ctx, int handle, int on);
 
 /*
  * Reads and clears the box's status word (no reference counterpart: the

@@ -52,8 +52,20 @@ __global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restri
     Uf[t] = (float)U[t];
 }
 
-// Interior cell t: its FP32 mirror, written to Uf from U, and its |v| + cs in
-// FP32; bad marks non-positive density or a non-finite value.
+// |v| + cs of one cell in FP32; bad marks non-positive density or a
+// non-finite value.
+template <int D>
+__device__ __forceinline__ float speed_f32(const MixedParams& M, const float* u, int& bad) {
+  float ss = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
+  const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
+  if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
+  return v;
+}
+
+// Interior cell t: its FP32 mirror, written to Uf from U, and its signal
+// speed.
 template <int D>
 __device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const double* __restrict__ U,
                                                   float* __restrict__ Uf, const Geom& g, long long t, int& bad) {
@@ -69,12 +81,88 @@ __device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const do
     u[c] = (float)U[(long long)c * g.field + o];
     Uf[(long long)c * g.field + o] = u[c];
   }
-  float ss = 0.f;
+  return speed_f32<D>(M, u, bad);
+}
+
+// Block-wide maximum and or of (m, bad), folded into *bits and *status by
+// one thread.
+__device__ __forceinline__ void block_fold(float m, int bad, unsigned long long* bits, int* status) {
 #pragma unroll
-  for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
-  const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
-  if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
-  return v;
+  for (int off = 16; off > 0; off >>= 1) {
+    const float o = __shfl_down_sync(0xffffffffu, m, off);
+    if (o > m) m = o;
+    bad |= __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  __shared__ float sm[kThreads / 32];
+  __shared__ int sb[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sm[warp] = m;
+    sb[warp] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < kThreads / 32; ++k) {
+      if (sm[k] > m) m = sm[k];
+      bad |= sb[k];
+    }
+    atomicMax(bits, (unsigned long long)__float_as_uint(m));
+    if (bad) atomicOr(status, 1);
+  }
+}
+
+// The arrival of rows [e0, e1) (elements of every component block; whole
+// rows of the outermost axis, ghosts included) of a box just copied into U:
+// the FP32 mirror Uf of every cell is written, the ghost cells are copied
+// into the other state buffer V, whose interior the next solve writes, and
+// the FP32 signal speed of every interior cell (the arithmetic of
+// cfl_f32_kernel) is folded into *bits, so that the CFL maximum is ready
+// when the last row has arrived.
+template <int D>
+__global__ void __launch_bounds__(kThreads)
+    ingest_kernel(MixedParams M, const double* __restrict__ U, double* __restrict__ V, float* __restrict__ Uf,
+                  Geom g, long long e0, long long e1, unsigned long long* bits, int* status) {
+  const long long F = g.field;
+  const long long E0 = g.s[1];                       // row length along x, ghosts included
+  const long long E1 = (D > 2) ? g.s[2] / g.s[1] : 1;  // rows per plane
+  float m = 0.f;
+  int bad = 0;
+  for (long long t = e0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; t < e1;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % E0);
+    const long long r = t / E0;
+    const int j = (D > 2) ? (int)(r % E1) : (int)r;
+    const int k = (D > 2) ? (int)(r / E1) : 0;
+    bool in = i >= 2 && i <= g.n[0] + 1;
+    if (D > 1) in = in && j >= 2 && j <= g.n[1] + 1;
+    if (D > 2) in = in && k >= 2 && k <= g.n[2] + 1;
+    float u[D + 2];
+#pragma unroll
+    for (int c = 0; c < D + 2; ++c) {
+      const double x = U[(long long)c * F + t];
+      u[c] = (float)x;
+      Uf[(long long)c * F + t] = u[c];
+      if (!in) V[(long long)c * F + t] = x;
+    }
+    if (in) {
+      const float v = speed_f32<D>(M, u, bad);
+      if (v > m) m = v;
+    }
+  }
+  block_fold(m, bad, bits, status);
+}
+
+// dt from a maximum folded by ingest_kernel: the last step of cfl_f32_kernel.
+__global__ void cfl_finish_kernel(const unsigned long long* __restrict__ bits, double courant, double mdx,
+                                  StepScratch s) {
+  const float mu = __uint_as_float((unsigned int)*bits);
+  const double dt = courant * mdx / (double)mu;
+  *s.dt = dt;
+  if (s.dt_trace) {
+    const int pos = *s.trace_pos;
+    if (pos >= 0 && pos < s.trace_cap) s.dt_trace[pos] = dt;
+    *s.trace_pos = pos + 1;
+  }
 }
 
 // FP32 mirror of the interior of U and its signal-speed maximum; the last
@@ -187,15 +275,18 @@ __device__ __forceinline__ void redo_any_axis(const MixedParams& M, int limiter,
 // FP64 redo of the queued interfaces; -+ dt/dx * F applied to the adjacent
 // interior cells of U^{n+1} (atomically: a cell can border two queued
 // interfaces).
+// Entries from *from (0 when from is null) to the queue's end: a solve in
+// slabs fixes the entries of each slab after its sweeps.
 template <int D>
 __global__ void __launch_bounds__(128)
     fallback_fix_kernel(MixedParams M, FallbackQueue q, Geom g, Dx dx, const double* __restrict__ dtp,
-                        const double* __restrict__ U, double* __restrict__ Unew) {
+                        const double* __restrict__ U, double* __restrict__ Unew, const int* __restrict__ from) {
   const int n = min(*q.n, q.cap);
-  if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(q.total, n);
+  const int lo = from ? min(*from, n) : 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n > lo) atomicAdd(q.total, n - lo);
   const double dt = *dtp;
   const long long F = g.field;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const FallbackEntry e = q.e[i];
     double f[D + 2];
     redo_any_axis<D>(M, M.limiter, M.omega64, U, g, e.axis, e.o, 0.5 * dt / dx.v[e.axis], f);
@@ -213,8 +304,9 @@ __global__ void __launch_bounds__(128)
 
 template <int D>
 cudaError_t launch_fallback(const MixedParams& M, const FallbackQueue& q, const Geom& g, const Dx& dx,
-                            const double* dtp, const double* U, double* Unew, cudaStream_t st) {
-  fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, g, dx, dtp, U, Unew);
+                            const double* dtp, const double* U, double* Unew, cudaStream_t st,
+                            const int* from = nullptr) {
+  fallback_fix_kernel<D><<<152, 128, 0, st>>>(M, q, g, dx, dtp, U, Unew, from);
   return cudaGetLastError();
 }
 
@@ -355,6 +447,47 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
   }
   if (e == cudaSuccess && ev) e = cudaEventRecord(ev[2], st);
   return e;
+}
+
+cudaError_t launch_mh_solve_mixed_slab(const MixedParams& M, const double* U, const float* Uf, double* Unew,
+                                       float* acc, const Geom& g, const Dx& dx, const StepScratch& s,
+                                       const FallbackQueue& q, int* done, const SweepPlan& plan, int lo, int hi,
+                                       cudaStream_t st) {
+  const int D = M.ndim;
+  if (D < 1 || D > 3) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+  for (int a = 0; a < D && e == cudaSuccess; ++a)
+    e = launch_sweep_slab(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, q, lo, hi, st);
+  if (e == cudaSuccess) {
+    switch (D) {
+      case 1: e = launch_fallback<1>(M, q, g, dx, s.dt, U, Unew, st, done); break;
+      case 2: e = launch_fallback<2>(M, q, g, dx, s.dt, U, Unew, st, done); break;
+      case 3: e = launch_fallback<3>(M, q, g, dx, s.dt, U, Unew, st, done); break;
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(done, q.n, sizeof(int), cudaMemcpyDeviceToDevice, st);
+  return e;
+}
+
+cudaError_t launch_ingest_mixed(const MixedParams& M, const double* U, double* V, float* Uf, const Geom& g,
+                                long long e0, long long e1, unsigned long long* bits, int* status,
+                                cudaStream_t st) {
+  if (e1 <= e0) return cudaSuccess;
+  int grid = grid_for(e1 - e0, kThreads);
+  if (grid > 152 * 8) grid = 152 * 8;
+  switch (M.ndim) {
+    case 1: ingest_kernel<1><<<grid, kThreads, 0, st>>>(M, U, V, Uf, g, e0, e1, bits, status); break;
+    case 2: ingest_kernel<2><<<grid, kThreads, 0, st>>>(M, U, V, Uf, g, e0, e1, bits, status); break;
+    case 3: ingest_kernel<3><<<grid, kThreads, 0, st>>>(M, U, V, Uf, g, e0, e1, bits, status); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cfl_finish(const unsigned long long* bits, double courant, const Dx& dx, const StepScratch& s,
+                              cudaStream_t st) {
+  cfl_finish_kernel<<<1, 1, 0, st>>>(bits, courant, dx.min, s);
+  return cudaGetLastError();
 }
 
 long long sweep_tile_count(int ndim, int axis, int shape, const int* n) {

@@ -52,6 +52,10 @@ struct FallbackQueue {
   int cap;
   int* status;  // bit 1: queue overflow
   int* total;   // running count of FP64 interfaces (statistics)
+  // A sweep over a slab of a box sees the box from the slab's first row
+  // (shifted pointers): its entries are shifted back by these.
+  long long o_base = 0;
+  int ga_base = 0;
 };
 
 // Tile shapes of the mixed sweeps, the autotuner's candidate set: S cells
@@ -155,6 +159,26 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
+// The mixed solve of the slab of interior cells [lo, hi] of the outermost
+// axis: its sweeps, then the FP64 fix-up of the queue entries from *done on,
+// after which *done is the queue's length. Solving every slab in order, with
+// *q.n and *done zeroed before the first, gives launch_mh_solve_mixed's
+// result. A slab's cells are final after its call except its last row: the
+// interface between it and the next slab's first row is queued for the FP64
+// fix-up (if at all) by the next slab.
+cudaError_t launch_mh_solve_mixed_slab(const MixedParams& M, const double* U, const float* Uf, double* Unew,
+                                       float* acc, const Geom& g, const Dx& dx, const StepScratch& s,
+                                       const FallbackQueue& q, int* done, const SweepPlan& plan, int lo, int hi,
+                                       cudaStream_t st);
+// Elements [e0, e1) of a box's component blocks just copied into U: their
+// FP32 mirror written to Uf, ghost cells copied into V, FP32 CFL maximum of
+// the interior folded into *bits (launch_cfl_finish turns it into dt as
+// launch_cfl_mixed would).
+cudaError_t launch_ingest_mixed(const MixedParams& M, const double* U, double* V, float* Uf, const Geom& g,
+                                long long e0, long long e1, unsigned long long* bits, int* status,
+                                cudaStream_t st);
+cudaError_t launch_cfl_finish(const unsigned long long* bits, double courant, const Dx& dx, const StepScratch& s,
+                              cudaStream_t st);
 
 // ---- batches of boxes (kernels_batch.cu) ---------------------------------
 // One entry of a batch's device box table, for one step parity: U is read,
@@ -202,12 +226,13 @@ struct BatchLists {
 // `shape` (the work items of a batch enumerate these).
 long long sweep_tile_count(int ndim, int axis, int shape, const int* n);
 
-// One mixed sweep of a box along `axis` with tile shape `shape`
-// (sweeps.cu, compiled once per dimensionality).
+// One mixed sweep along `axis` with tile shape `shape` of the slab of a box
+// holding interior cells [lo, hi] of its outermost axis (sweeps.cu, compiled
+// once per dimensionality).
 #define RGPU_SWEEP_DECL(D)                                                                              \
   cudaError_t launch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const float* Uf,         \
                                     const double* U, const Geom& g, const Dx& dx, const double* dtp,    \
-                                    float* acc, double* Unew, const FallbackQueue& q,                   \
+                                    float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,   \
                                     cudaStream_t st);                                                   \
   cudaError_t launch_batch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const BoxDesc* TB, \
                                           const WorkItem* items, int n, int* head, const FallbackQueue& q, \
@@ -217,15 +242,24 @@ RGPU_SWEEP_DECL(2)
 RGPU_SWEEP_DECL(3)
 #undef RGPU_SWEEP_DECL
 
+inline cudaError_t launch_sweep_slab(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
+                                     const double* U, const Geom& g, const Dx& dx, const double* dtp,
+                                     float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,
+                                     cudaStream_t st) {
+  switch (ndim) {
+    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// The sweep over the whole box.
 inline cudaError_t launch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
                                      const double* U, const Geom& g, const Dx& dx, const double* dtp,
                                      float* acc, double* Unew, const FallbackQueue& q, cudaStream_t st) {
-  switch (ndim) {
-    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-    default: return cudaErrorInvalidValue;
-  }
+  if (ndim < 1 || ndim > 3) return cudaErrorInvalidValue;
+  return launch_sweep_slab(ndim, axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, 1, g.n[ndim - 1], st);
 }
 
 inline cudaError_t launch_batch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M,

@@ -24,6 +24,11 @@ using namespace rgpu;
 
 namespace {
 
+// Slabs of an overlapped upload or solve, and the smallest box (hydro bytes)
+// worth it.
+constexpr int kPipeSlabs = 16;
+constexpr size_t kPipeMinBytes = size_t(16) << 20;
+
 struct Box {
   int level = 0, number = 0;
   double* host = nullptr;
@@ -50,6 +55,20 @@ struct Box {
   Dx dx{};          // cell size for batched steps (rhyme_gpu_batch_create)
   SweepPlan plan{};  // tile shape per axis of the mixed sweeps
   bool plan_valid = false;
+  // Copies overlapped with kernels (2-/3-D mixed boxes with a page-locked
+  // host array): an upload writes the FP32 mirror of the arriving rows
+  // (mirror_valid: Uf[cur] is the FP32 image of the current state, as long
+  // as ghost fills keep the two in step) and folds their CFL maximum into
+  // *ingest_bits (maxu_valid: it is the current state's), and with
+  // write-back on (wb) a solve copies the rows of the new state to the host
+  // array as they are finished (wb_pending: the host array receives the
+  // current state).
+  unsigned long long* ingest_bits = nullptr;
+  int* fb_done = nullptr;  // fix-up entries done by the slabs solved so far
+  bool mirror_valid = false;
+  bool maxu_valid = false;
+  bool wb = false;
+  bool wb_pending = false;
 };
 
 }  // namespace
@@ -76,6 +95,9 @@ struct rhyme_gpu_ctx {
   PackDesc* out_desc = nullptr;
   size_t desc_cap = 0;  // descriptors
   bool out_pending = false;
+  // slab pipelines of uploads and write-backs (on the copy stream)
+  cudaEvent_t pipe_ev[kPipeSlabs + 1] = {};
+  cudaEvent_t wb_done = nullptr;
 };
 
 namespace {
@@ -293,6 +315,9 @@ int rhyme_gpu_destroy(rhyme_gpu_ctx* ctx) {
   cudaFree(ctx->out_desc);
   if (ctx->out_packed) cudaEventDestroy(ctx->out_packed);
   if (ctx->out_done) cudaEventDestroy(ctx->out_done);
+  for (cudaEvent_t ev : ctx->pipe_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->wb_done) cudaEventDestroy(ctx->wb_done);
   if (ctx->copy) cudaStreamDestroy(ctx->copy);
   cudaFreeHost(ctx->pinned_dt);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -330,6 +355,69 @@ long long box_device_bytes(int D, bool mixed, const int* dims) {
     bytes += 3LL * D * (D + 2) * F * 8;
   }
   return bytes;
+}
+
+// The copy stream and its events, made on first use.
+int ensure_copy_stream(rhyme_gpu_ctx* ctx) {
+  if (ctx->copy) return RHYME_GPU_OK;
+  CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->out_packed, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->out_done, cudaEventDisableTiming));
+  for (cudaEvent_t& ev : ctx->pipe_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->wb_done, cudaEventDisableTiming));
+  return RHYME_GPU_OK;
+}
+
+// The state of the box changed on the device: the upload's CFL maximum and
+// the write-back no longer describe it.
+void state_changed(Box* b) {
+  b->mirror_valid = false;
+  b->maxu_valid = false;
+  b->wb_pending = false;
+}
+
+// Whether the box's copies overlap its kernels: mixed precision, 2-D or 3-D,
+// a host array the library page-locked, and enough rows of the outermost
+// axis to split.
+bool pipelined(const rhyme_gpu_ctx* ctx, const Box* b) {
+  const int D = ctx->params.ndim;
+  return ctx->mixed && D >= 2 && b->registered_host && b->hydro_bytes >= kPipeMinBytes &&
+         b->g.n[D - 1] >= 2 * kPipeSlabs;
+}
+
+// Upload in slabs of rows of the outermost axis (copy stream); each slab,
+// once arrived, has its ghost cells copied to the other buffer and the CFL
+// maximum of its interior folded into *ingest_bits (context stream), while
+// the next slab is in flight.
+int upload_slabs(rhyme_gpu_ctx* ctx, Box* b) {
+  int rc = ensure_copy_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  const int D = ctx->params.ndim, O = D - 1;
+  const long long row = b->g.s[O];
+  const int rows = b->g.n[O] + 4;
+  const size_t pitch = (size_t)b->g.field * sizeof(double);
+  double* U = b->state[b->cur];
+  double* V = b->state[1 - b->cur];
+  state_changed(b);
+  // the copies follow the context stream's earlier work on these buffers
+  CK(cudaEventRecord(ctx->pipe_ev[kPipeSlabs], ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->copy, ctx->pipe_ev[kPipeSlabs], 0));
+  CK(cudaMemsetAsync(b->ingest_bits, 0, sizeof(unsigned long long), ctx->stream));
+  const int per = (rows + kPipeSlabs - 1) / kPipeSlabs;
+  for (int j = 0; j < kPipeSlabs; ++j) {
+    const int r0 = j * per, r1 = std::min(rows, r0 + per);
+    if (r0 >= r1) break;
+    const size_t off = (size_t)r0 * row;
+    CK(cudaMemcpy2DAsync(U + off, pitch, b->host + off, pitch, (size_t)(r1 - r0) * row * sizeof(double), D + 2,
+                         cudaMemcpyHostToDevice, ctx->copy));
+    CK(cudaEventRecord(ctx->pipe_ev[j], ctx->copy));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->pipe_ev[j], 0));
+    CK(launch_ingest_mixed(b->mp, U, V, b->Uf[b->cur], b->g, (long long)off, (long long)r1 * row, b->ingest_bits,
+                           b->s.status, ctx->stream));
+  }
+  b->mirror_valid = true;
+  b->maxu_valid = true;
+  return RHYME_GPU_OK;
 }
 
 int register_box_impl(rhyme_gpu_ctx* ctx, int level, int number, double* cells, const int dims[3], int ghost,
@@ -385,6 +473,8 @@ int register_box_impl(rhyme_gpu_ctx* ctx, int level, int number, double* cells, 
   b->trace_pos = (int*)(base + 24);
   b->fb_count = (int*)(base + 28);
   b->fbq.n = (int*)(base + 32);
+  b->fb_done = (int*)(base + 36);
+  b->ingest_bits = (unsigned long long*)(base + 40);
   b->fbq.status = b->s.status;
   b->fbq.total = b->fb_count;
   b->trace_buf = (double*)(base + 64);
@@ -428,6 +518,12 @@ int rhyme_gpu_unregister_box(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  // copies to or from the host array may be in flight (the context stream
+  // waits for them)
+  if (b->registered_host) {
+    int rc = wait_stream(ctx);
+    if (rc != RHYME_GPU_OK) return rc;
+  }
   destroy_box(b, ctx->stream);
   ctx->boxes[handle] = nullptr;
   return RHYME_GPU_OK;
@@ -437,6 +533,8 @@ int rhyme_gpu_sync_to_device(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  if (pipelined(ctx, b)) return upload_slabs(ctx, b);
+  state_changed(b);
   // Both buffers receive the full hydro blocks (ghosts and corners included).
   CK(cudaMemcpyAsync(b->state[b->cur], b->host, b->hydro_bytes, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(b->state[1 - b->cur], b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToDevice,
@@ -454,8 +552,18 @@ int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle) {
   if (!ctx) return RHYME_GPU_EINVAL;
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
-  CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  // with write-back the solve's copies are in flight (the stream waits for them)
+  if (!b->wb_pending)
+    CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return wait_stream(ctx);
+}
+
+int rhyme_gpu_set_host_writeback(rhyme_gpu_ctx* ctx, int handle, int on) {
+  if (!ctx) return RHYME_GPU_EINVAL;
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  b->wb = on != 0;
+  return RHYME_GPU_OK;
 }
 
 int rhyme_gpu_box_status(rhyme_gpu_ctx* ctx, int handle, int* flags) {
@@ -522,6 +630,7 @@ int tune_axis(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx, int axis, int* best) {
   *best = default_sweep_shape(D, axis, b->g.n[axis]);
   CK(launch_cfl_mixed(b->mp, b->state[c], b->Uf[c], b->g, b->dp.courant, dx, sc, ctx->stream));
   CK(launch_ghost_fill_f32(b->dp, b->Uf[c], b->g, ctx->stream));
+  b->mirror_valid = false;  // the FP32 ghosts were filled without the FP64 ones
   cudaEvent_t ev[2];
   CK(cudaEventCreate(&ev[0]));
   if (cudaEventCreate(&ev[1]) != cudaSuccess) {
@@ -639,6 +748,53 @@ int ensure_graphs(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
   return RHYME_GPU_OK;
 }
 
+// The mixed solve in slabs of rows of the outermost axis (a multiple of
+// every sweep's tile extent along it), each slab's finished rows copied to
+// the host array on the copy stream while the next slab is solved. A slab's
+// last row waits for the next slab, which may queue the FP64 fix-up of the
+// interface between them. The context stream waits for the copies.
+int solve_slabs_write_back(rhyme_gpu_ctx* ctx, Box* b, const Dx& d) {
+  int rc = ensure_copy_stream(ctx);
+  if (rc != RHYME_GPU_OK) return rc;
+  const int D = ctx->params.ndim, O = D - 1;
+  const int N = b->g.n[O];
+  int align = 1;
+  for (int a = 0; a < D; ++a) {
+    int S = 1, P = 1;
+    sweep_shape(D, b->plan.shape[a], &S, &P);
+    const int bax = (a == 0) ? 1 : 0;
+    const int t = (a == O) ? S : (bax == O ? P : 1);
+    if (t > align) align = t;
+  }
+  int rows = (N + kPipeSlabs - 1) / kPipeSlabs;
+  rows = (rows + align - 1) / align * align;
+  const long long row = b->g.s[O];
+  const size_t pitch = (size_t)b->g.field * sizeof(double);
+  const double* U = b->state[b->cur];
+  double* V = b->state[1 - b->cur];
+  const StepScratch sc = scratch_of(b, false);
+  CK(cudaMemsetAsync(b->fbq.n, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(b->fb_done, 0, sizeof(int), ctx->stream));
+  long long copied = 0;  // array rows of V already sent
+  int j = 0;
+  for (int lo = 1; lo <= N; lo += rows, ++j) {
+    const int hi = std::min(N, lo + rows - 1);
+    CK(launch_mh_solve_mixed_slab(b->mp, U, b->Uf[b->cur], V, b->acc, b->g, d, sc, b->fbq, b->fb_done, b->plan,
+                                  lo, hi, ctx->stream));
+    // final: array rows up to the one of cell hi - 1 (cell i is array row
+    // i + 1), or all of them after the last slab
+    const long long end = (hi == N) ? (long long)N + 4 : (long long)hi + 1;
+    CK(cudaEventRecord(ctx->pipe_ev[j], ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->copy, ctx->pipe_ev[j], 0));
+    CK(cudaMemcpy2DAsync(b->host + copied * row, pitch, V + copied * row, pitch,
+                         (size_t)((end - copied) * row) * sizeof(double), D + 2, cudaMemcpyDeviceToHost, ctx->copy));
+    copied = end;
+  }
+  CK(cudaEventRecord(ctx->wb_done, ctx->copy));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->wb_done, 0));
+  return RHYME_GPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -648,7 +804,9 @@ int rhyme_gpu_cfl_time_step(rhyme_gpu_ctx* ctx, int handle, const double dx[3], 
   Box* b = find_box(ctx, handle);
   if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
   Dx d = make_dx(ctx->params.ndim, dx);
-  if (ctx->mixed)
+  if (ctx->mixed && b->maxu_valid)
+    CK(launch_cfl_finish(b->ingest_bits, b->dp.courant, d, scratch_of(b, false), ctx->stream));
+  else if (ctx->mixed)
     CK(launch_cfl_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->g, b->dp.courant, d, scratch_of(b, false),
                         ctx->stream));
   else
@@ -689,18 +847,34 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   if (rc != RHYME_GPU_OK) return rc;
   ctx->pinned_dt[0] = dt;
   CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  bool written_back = false;
   if (ctx->mixed) {
     // the FP32 mirror of the whole box (ghosts included) from the state this
-    // solve reads: a driver may call the solve without the CFL pass that
-    // otherwise writes the mirror
-    CK(launch_to_f32(b->state[b->cur], b->Uf[b->cur], (long long)(ctx->params.ndim + 2) * b->g.field, ctx->stream));
-    CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->acc, b->g, d,
-                             scratch_of(b, false), b->fbq, b->plan, ctx->stream));
+    // solve reads, unless an upload wrote it since the state last changed
+    // (the ghost fill keeps it in step): a driver may call the solve without
+    // the CFL pass that otherwise writes the mirror
+    if (!b->mirror_valid)
+      CK(launch_to_f32(b->state[b->cur], b->Uf[b->cur], (long long)(ctx->params.ndim + 2) * b->g.field,
+                       ctx->stream));
+    if (b->wb && pipelined(ctx, b)) {
+      rc = solve_slabs_write_back(ctx, b, d);
+      if (rc != RHYME_GPU_OK) return rc;
+      written_back = true;
+    } else {
+      CK(launch_mh_solve_mixed(b->mp, b->state[b->cur], b->Uf[b->cur], b->state[1 - b->cur], b->acc, b->g, d,
+                               scratch_of(b, false), b->fbq, b->plan, ctx->stream));
+    }
   }
   else
     CK(launch_mh_solve(b->dp, b->state[b->cur], b->state[1 - b->cur], b->g, d, scratch_of(b, false),
                        ctx->stream));
   b->cur = 1 - b->cur;
+  state_changed(b);
+  if (b->wb) {
+    if (!written_back)
+      CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    b->wb_pending = true;
+  }
   return RHYME_GPU_OK;
 }
 
@@ -712,6 +886,7 @@ int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int nsteps
   Dx d = make_dx(ctx->params.ndim, dx);
   int rc = ensure_graphs(ctx, b, d);
   if (rc != RHYME_GPU_OK) return rc;
+  if (nsteps > 0) state_changed(b);
   int done = 0;
   while (done < nsteps) {
     const int chunk = (nsteps - done < kTraceCap) ? nsteps - done : kTraceCap;
@@ -852,6 +1027,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   Dx d = make_dx(ctx->params.ndim, dx);
   int prc = box_plan(ctx, b, d);
   if (prc != RHYME_GPU_OK) return prc;
+  state_changed(b);
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
   double acc[5] = {0, 0, 0, 0, 0};
@@ -937,10 +1113,9 @@ extern "C" int rhyme_gpu_output_level(rhyme_gpu_ctx* ctx, const int* handles, in
   }
   if (capacity < out_len)
     return fail(ctx, RHYME_GPU_EINVAL, "output holds %lld values, the level needs %lld", capacity, out_len);
-  if (!ctx->copy) {
-    CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&ctx->out_packed, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ctx->out_done, cudaEventDisableTiming));
+  {
+    int rc = ensure_copy_stream(ctx);
+    if (rc != RHYME_GPU_OK) return rc;
   }
   // the staging buffers of an earlier output are reused once its copies ended
   if (ctx->out_pending) {
@@ -1140,6 +1315,7 @@ extern "C" int rhyme_gpu_paint(rhyme_gpu_ctx* ctx, int handle, const int left_ed
   std::vector<PaintShape> ps;
   int rc = make_paint_shapes(ctx, b, left_edge, shapes, n, &ps);
   if (rc != RHYME_GPU_OK) return rc;
+  state_changed(b);
   PaintShape* d = nullptr;
   CK(cudaMallocAsync((void**)&d, sizeof(PaintShape) * n, ctx->stream));
   cudaError_t e = cudaMemcpyAsync(d, ps.data(), sizeof(PaintShape) * n, cudaMemcpyHostToDevice, ctx->stream);
@@ -1446,7 +1622,11 @@ extern "C" int rhyme_gpu_batch_run(rhyme_gpu_batch* B, int nsteps) {
                            ctx->stream));
     B->k ^= 1;
   }
-  for (size_t i = 0; i < B->handles.size(); ++i) ctx->boxes[B->handles[i]]->cur = B->base_cur[i] ^ B->k;
+  for (size_t i = 0; i < B->handles.size(); ++i) {
+    Box* b = ctx->boxes[B->handles[i]];
+    b->cur = B->base_cur[i] ^ B->k;
+    if (nsteps > 0) state_changed(b);
+  }
   return RHYME_GPU_OK;
 }
 

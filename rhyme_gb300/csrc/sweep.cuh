@@ -182,9 +182,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
         if (slot < q.cap) {
           FallbackEntry& e = q.e[slot];
           e.axis = A;
-          e.ga = ga;
+          e.ga = ga + q.ga_base;
           e.box = box;
-          e.o = offset(ga, b0 + lb);
+          e.o = offset(ga, b0 + lb) + q.o_base;
         } else {
           atomicOr(q.status, 2);  // queue full: the interface keeps a zero flux
         }

@@ -18,18 +18,41 @@ constexpr int mode_of() {
   return D == 1 ? ONLY : (A == 0 ? FIRST : (A == D - 1 ? LAST : MID));
 }
 
+// The tiles covering interior cells [lo, hi] of the outermost axis O = D-1
+// (the whole box for lo = 1, hi = n[O]). A slab is swept as a box that
+// starts at its first row: pointers shifted by lo - 1 rows, the extent along
+// O cut to the rows from lo on (the rows before and after stay readable as
+// the stencil's halo), queue entries shifted back. Where the tiles span O
+// (O = A, or O = B across the pencils) the slab must start on a tile
+// boundary and end on one or at the box's edge, so that every cell belongs
+// to exactly one slab.
 template <int D, int A, int S, int P>
 cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, const Geom& g, const Dx& dx,
-                       const double* dtp, float* acc, double* Unew, const FallbackQueue& q,
+                       const double* dtp, float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,
                        cudaStream_t st) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
-  const int NA = g.n[A];
-  const int NB = (B < D) ? g.n[B] : 1;
-  const int NC = (C < D) ? g.n[C] : 1;
+  constexpr int O = D - 1;
+  const int NO = g.n[O];
+  if (lo < 1 || hi > NO || lo > hi) return cudaErrorInvalidValue;
+  if (O == A || O == B) {
+    constexpr int T = (O == A) ? S : P;
+    if ((lo - 1) % T != 0 || (hi != NO && (hi - lo + 1) % T != 0)) return cudaErrorInvalidValue;
+  }
+  Geom gs = g;
+  FallbackQueue qs = q;
+  const long long shift = (long long)(lo - 1) * g.s[O];
+  gs.n[O] = NO - (lo - 1);
+  qs.o_base = shift;
+  qs.ga_base = (O == A) ? lo - 1 : 0;
+  const int rows = hi - lo + 1;
+  const int NA = (O == A) ? rows : g.n[A];
+  const int NB = (B < D) ? ((O == B) ? rows : g.n[B]) : 1;
+  const int NC = (C < D) ? ((O == C) ? rows : g.n[C]) : 1;
   const int tA = (NA + S - 1) / S, tB = (NB + P - 1) / P;
   if ((A == 0 ? tB : tA) > 65535 || NC > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid = (A == 0) ? dim3(tA, tB, NC) : dim3(tB, tA, NC);
-  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(M, Uf, U, g, dx, dtp, acc, Unew, q);
+  sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(
+      M, Uf + shift, U + shift, gs, dx, dtp, acc + shift, Unew + shift, qs);
   return cudaGetLastError();
 }
 
@@ -45,20 +68,20 @@ cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const Work
 template <int D, int A>
 cudaError_t by_shape(int shape, const MixedParams& M, const float* Uf, const double* U, const Geom& g,
                      const Dx& dx, const double* dtp, float* acc, double* Unew,
-                     const FallbackQueue& q, cudaStream_t st) {
+                     const FallbackQueue& q, int lo, int hi, cudaStream_t st) {
   if constexpr (D == 1) {
     switch (shape) {
-      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
     }
   } else {
     switch (shape) {
-      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
-      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
     }
   }
   return cudaErrorInvalidValue;
@@ -93,15 +116,15 @@ cudaError_t batch_by_shape(int shape, const MixedParams& M, const BoxDesc* TB, c
 cudaError_t RGPU_CAT(launch_sweep_axis_, SWEEP_D)(int axis, int shape, const MixedParams& M, const float* Uf,
                                                  const double* U, const Geom& g, const Dx& dx,
                                                  const double* dtp, float* acc, double* Unew,
-                                                 const FallbackQueue& q, cudaStream_t st) {
+                                                 const FallbackQueue& q, int lo, int hi, cudaStream_t st) {
   constexpr int D = SWEEP_D;
   switch (axis) {
-    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
     case 1:
-      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
       break;
     case 2:
-      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, st);
+      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
       break;
   }
   return cudaErrorInvalidValue;

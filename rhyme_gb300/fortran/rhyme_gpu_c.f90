@@ -89,6 +89,12 @@ module rhyme_gpu_c
          integer(c_int), value :: handle
       end function rhyme_gpu_sync_to_host
 
+      integer(c_int) function rhyme_gpu_set_host_writeback(ctx, handle, on) bind(c, name='rhyme_gpu_set_host_writeback')
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: handle, on
+      end function rhyme_gpu_set_host_writeback
+
       integer(c_int) function rhyme_gpu_box_status(ctx, handle, flags) bind(c, name='rhyme_gpu_box_status')
          import :: c_int, c_ptr
          type(c_ptr), value :: ctx

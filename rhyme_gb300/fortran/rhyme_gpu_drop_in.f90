@@ -107,6 +107,11 @@ contains
          return
       end if
       rhyme_gpu_handles(box%level, box%number) = h
+      ! host-authoritative: each solve copies its result back while it runs
+      if (.not. rhyme_gpu_device_resident) then
+         rc = rhyme_gpu_set_host_writeback(rhyme_gpu_ctx_ptr, h, 1_c_int)
+         if (rc /= rhyme_gpu_ok) call logger%err('rhyme_gpu_set_host_writeback failed')
+      end if
    end subroutine rhyme_gpu_drop_in_register
 
    pure integer(c_int) function rhyme_gpu_handle_of(box) result(h)

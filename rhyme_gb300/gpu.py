@@ -27,7 +27,8 @@ _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMED
 # Every symbol include/rhyme_gpu.h declares.
 EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rhyme_gpu_last_error",
            "rhyme_gpu_get_stream", "rhyme_gpu_register_box", "rhyme_gpu_unregister_box",
-           "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_cfl_time_step", "rhyme_gpu_cfl_dt",
+           "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_set_host_writeback",
+           "rhyme_gpu_cfl_time_step", "rhyme_gpu_cfl_dt",
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
@@ -141,6 +142,7 @@ def load():
     L.rhyme_gpu_unregister_box.argtypes = [vp, C.c_int]
     L.rhyme_gpu_sync_to_device.argtypes = [vp, C.c_int]
     L.rhyme_gpu_sync_to_host.argtypes = [vp, C.c_int]
+    L.rhyme_gpu_set_host_writeback.argtypes = [vp, C.c_int, C.c_int]
     L.rhyme_gpu_cfl_time_step.argtypes = [vp, C.c_int, dp, dp]
     L.rhyme_gpu_set_boundaries.argtypes = [vp, C.c_int]
     L.rhyme_gpu_cfl_dt.argtypes = [vp, C.c_int, dp]
@@ -301,6 +303,12 @@ class Context:
 
     def sync_to_host(self, box):
         self._check(self.lib.rhyme_gpu_sync_to_host(self.h, box.handle))
+
+    def set_host_writeback(self, box, on=True):
+        """Each solve of the box also copies the new state into its cells
+        array (overlapped with the solve for large 2-/3-D mixed boxes);
+        sync_to_host then only waits for those copies."""
+        self._check(self.lib.rhyme_gpu_set_host_writeback(self.h, box.handle, 1 if on else 0))
 
     def box_status(self, box):
         """Status bits of the box since the last query (0 = clean)."""
