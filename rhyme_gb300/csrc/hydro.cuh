@@ -344,16 +344,22 @@ struct Star {
   bool converged;  // first guess met the tolerance
 };
 
-// rhyme_riemann_problem_star.f90:12-65
+// rhyme_riemann_problem_star.f90:12-65, split so that only the side the
+// sampling reads is formed: p* and u* (:12-38), then the left (:40, 43-53)
+// or the right (:41, 55-65) star state, each with the reference's
+// operations.
 template <int D, int AX, typename T>
-__device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
-                                        const Side<D, T>& R, Star<T>& s) {
+__device__ __forceinline__ void rp_star_pu(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
+                                           const Side<D, T>& R, Star<T>& s) {
   s.p = irs_exec(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
                  s.r_f, &s.converged);
   if (s.p < rp.vac_p) s.p = rp.vac_p;
   s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
+}
+
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_star_left(const Gas<T>& G, const Side<D, T>& L, Star<T>& s) {
   T ps_pl = s.p / L.p;
-  T ps_pr = s.p / R.p;
   if (s.p > L.p) {
     s.l_shock = true;
     s.l_rho = L.rho * (G.gm1_gp1 + ps_pl) / (G.gm1_gp1 * ps_pl + T(1));
@@ -367,6 +373,11 @@ __device__ __forceinline__ void rp_star(const Gas<T>& G, const Rp<T>& rp, const 
     s.l_speedH = L.v[AX] - L.cs;
     s.l_speedT = s.u - s.l_cs;
   }
+}
+
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_star_right(const Gas<T>& G, const Side<D, T>& R, Star<T>& s) {
+  T ps_pr = s.p / R.p;
   if (s.p > R.p) {
     s.r_shock = true;
     s.r_rho = R.rho * (G.gm1_gp1 + ps_pr) / (G.gm1_gp1 * ps_pr + T(1));
@@ -410,10 +421,13 @@ __device__ __forceinline__ void w_star(const Gas<T>& G, const Side<D, T>& side, 
 }
 
 // rhyme_riemann_problem_sampling.f90:13-47 at x/t = dxdt
+// (the reference forms both sides' star states first; only the side read
+// here is formed, which leaves every value read unchanged)
 template <int D, int AX, typename T>
 __device__ __forceinline__ void rp_sampling(const Gas<T>& G, const Side<D, T>& L, const Side<D, T>& R,
-                                            const Star<T>& s, T dxdt, T* u) {
+                                            Star<T>& s, T dxdt, T* u) {
   if (dxdt > s.u) {
+    rp_star_right<D, AX>(G, R, s);
     if (s.r_shock) {
       if (dxdt < s.r_speed) w_star<D, AX>(G, R, s, s.r_rho, u);
       else prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
@@ -423,6 +437,7 @@ __device__ __forceinline__ void rp_sampling(const Gas<T>& G, const Side<D, T>& L
       else prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
     }
   } else {
+    rp_star_left<D, AX>(G, L, s);
     if (s.l_shock) {
       if (dxdt > s.l_speed) w_star<D, AX>(G, L, s, s.l_rho, u);
       else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
@@ -525,7 +540,7 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       }
     } else {
       Star<T> s;
-      rp_star<D, AX>(G, rp, L, R, s);
+      rp_star_pu<D, AX>(G, rp, L, R, s);
       if (CHECK && !s.converged) {
         *need64 = true;
         return;
