@@ -207,11 +207,28 @@ __device__ __forceinline__ void face_states(const Gas<T>& G, int lim, T w, const
 // Loop-invariant terms of rhyme_irs_nonlinear_wave_function.f90:15-23 for one
 // side (Ak, Bk, 2cs/gm1, 1/(rho cs)): the reference recomputes them every
 // Newton iteration with the same operations, so computing them once gives the
-// same values.
+// same values. In double the pair a branch needs is formed on its first use
+// (a side usually stays a shock or a rarefaction through the iteration, and
+// FP64 divisions are scarce on GB300); in float all four up front.
 template <typename T>
 struct WaveSide {
   T rho, p, cs, Ak, Bk, c2g, irc;
+  bool shock_ready, fan_ready;
 };
+
+template <typename T>
+__device__ __forceinline__ void wave_shock_terms(const Gas<T>& G, WaveSide<T>& w) {
+  w.Ak = T(2) / (G.gp1 * w.rho);
+  w.Bk = G.gm1 * w.p / G.gp1;
+  w.shock_ready = true;
+}
+
+template <typename T>
+__device__ __forceinline__ void wave_fan_terms(const Gas<T>& G, WaveSide<T>& w) {
+  w.c2g = T(2) * w.cs / G.gm1;
+  w.irc = T(1) / (w.rho * w.cs);
+  w.fan_ready = true;
+}
 
 template <typename T>
 __device__ __forceinline__ WaveSide<T> wave_side(const Gas<T>& G, T s_rho, T s_p, T s_cs) {
@@ -219,18 +236,21 @@ __device__ __forceinline__ WaveSide<T> wave_side(const Gas<T>& G, T s_rho, T s_p
   w.rho = s_rho;
   w.p = s_p;
   w.cs = s_cs;
-  w.Ak = T(2) / (G.gp1 * s_rho);
-  w.Bk = G.gm1 * s_p / G.gp1;
-  w.c2g = T(2) * s_cs / G.gm1;
-  w.irc = T(1) / (s_rho * s_cs);
+  w.shock_ready = w.fan_ready = false;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    wave_shock_terms(G, w);
+    wave_fan_terms(G, w);
+  }
   return w;
 }
 
 // rhyme_irs_nonlinear_wave_function.f90:13-24
 template <typename T>
-__device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, const WaveSide<T>& w, T p, T& f,
-                                               T& fprime) {
+__device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, WaveSide<T>& w, T p, T& f, T& fprime) {
   if (p > w.p) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+      if (!w.shock_ready) wave_shock_terms(G, w);
+    }
     const T bp = w.Bk + p;
     const T factor = m_sqrt(w.Ak / bp);
     f = (p - w.p) * factor;
@@ -244,6 +264,7 @@ __device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, const WaveSide<T
     f = w.c2g * expm1f(G.gm1_2g * t);
     fprime = w.irc * expf(-G.gp1_2g * t);
   } else {
+    if (!w.fan_ready) wave_fan_terms(G, w);
     T y, z;
     m_pow2(p / w.p, G.gm1_2g, -G.gp1_2g, y, z);
     f = w.c2g * (y - T(1));
@@ -305,8 +326,8 @@ __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rh
                                       bool* converged = nullptr) {
   T p_star = T(0), p_prev, l_fp, r_fp;
   if (converged) *converged = false;
-  const WaveSide<T> WL = wave_side(G, l_rho, l_p, l_cs);
-  const WaveSide<T> WR = wave_side(G, r_rho, r_p, r_cs);
+  WaveSide<T> WL = wave_side(G, l_rho, l_p, l_cs);
+  WaveSide<T> WR = wave_side(G, r_rho, r_p, r_cs);
   for (int gid = 0; gid < 6; ++gid) {
     p_star = guess_p_star(G, gid, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
     p_prev = p_star;
@@ -421,12 +442,21 @@ __device__ __forceinline__ void w_star(const Gas<T>& G, const Side<D, T>& side, 
 }
 
 // rhyme_riemann_problem_sampling.f90:13-47 at x/t = dxdt
-// (the reference forms both sides' star states first; only the side read
-// here is formed, which leaves every value read unchanged)
+// (the reference forms both sides' star states, and both sides' velocities
+// across AX, first; only the side read here gets them, from its conserved
+// state q, which leaves every value read unchanged)
 template <int D, int AX, typename T>
-__device__ __forceinline__ void rp_sampling(const Gas<T>& G, const Side<D, T>& L, const Side<D, T>& R,
-                                            Star<T>& s, T dxdt, T* u) {
+__device__ __forceinline__ void side_transverse(Side<D, T>& S, const T* q) {
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    if (a != AX) S.v[a] = q[1 + a] / q[0];
+}
+
+template <int D, int AX, typename T>
+__device__ __forceinline__ void rp_sampling(const Gas<T>& G, Side<D, T>& L, Side<D, T>& R, const T* l,
+                                            const T* r, Star<T>& s, T dxdt, T* u) {
   if (dxdt > s.u) {
+    side_transverse<D, AX>(R, r);
     rp_star_right<D, AX>(G, R, s);
     if (s.r_shock) {
       if (dxdt < s.r_speed) w_star<D, AX>(G, R, s, s.r_rho, u);
@@ -437,6 +467,7 @@ __device__ __forceinline__ void rp_sampling(const Gas<T>& G, const Side<D, T>& L
       else prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
     }
   } else {
+    side_transverse<D, AX>(L, l);
     rp_star_left<D, AX>(G, L, s);
     if (s.l_shock) {
       if (dxdt > s.l_speed) w_star<D, AX>(G, L, s, s.l_rho, u);
@@ -508,16 +539,13 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
   } else if (vacuum_both) {
     vacuum_state<D>(G, rp, u);
   } else {
-#pragma unroll
-    for (int a = 0; a < D; ++a) L.v[a] = l[1 + a] / l[0];
+    // velocities across AX: only for the side sampled (side_transverse)
+    L.v[AX] = l[1 + AX] / l[0];
     L.p = fmax_ref(pressure<D>(G, l), rp.vac_p);
     L.cs = fmax_ref(sound_speed<D>(G, l), tiny);
-#pragma unroll
-    for (int a = 0; a < D; ++a) R.v[a] = r[1 + a] / r[0];
+    R.v[AX] = r[1 + AX] / r[0];
     R.p = fmax_ref(pressure<D>(G, r), rp.vac_p);
     R.cs = fmax_ref(sound_speed<D>(G, r), tiny);
-    T s_starl = L.v[AX] - T(2) * L.cs / G.gm1;
-    T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
     T du = R.v[AX] - L.v[AX];
     T du_crit = T(2) * (L.cs + R.cs) / G.gm1;
     if (CHECK) {
@@ -529,12 +557,16 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       }
     }
     if (du_crit < du) {  // vacuum generation
+      const T s_starl = L.v[AX] - T(2) * L.cs / G.gm1;
+      const T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
       if (dxdt > s_starr) {
+        side_transverse<D, AX>(R, r);
         if (dxdt > R.v[AX] + R.cs) prim_vars_to_cons<D>(G, R.rho, R.v, R.p, u);
         else w_kfan<D, AX>(G, R, dxdt, true, u);
       } else if (dxdt > s_starl) {
         vacuum_state<D>(G, rp, u);
       } else {
+        side_transverse<D, AX>(L, l);
         if (dxdt > L.v[AX] - L.cs) w_kfan<D, AX>(G, L, dxdt, false, u);
         else prim_vars_to_cons<D>(G, L.rho, L.v, L.p, u);
       }
@@ -545,7 +577,7 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
         *need64 = true;
         return;
       }
-      rp_sampling<D, AX>(G, L, R, s, dxdt, u);
+      rp_sampling<D, AX>(G, L, R, l, r, s, dxdt, u);
     }
   }
 }

@@ -132,8 +132,10 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// At least 3 CTAs per SM: the persistent grid is 152 x 3 CTAs (and in 3-D
+// the FP64 solver would otherwise take 216 registers, 2 CTAs per SM).
 template <int D>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 3)
     batch_flux_kernel(Gas<double> G, Rp<double> rp, const BoxDesc* __restrict__ TB,
                       const WorkItem* __restrict__ items, int n, int* head) {
   for (int it = next_item(head, n); it >= 0; it = next_item(head, n)) {

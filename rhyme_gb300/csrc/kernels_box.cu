@@ -144,8 +144,8 @@ __global__ void __launch_bounds__(kFaceBlock)
 
 // Pass 2: exact Riemann problem and flux of every interface, i_AX in [0, N].
 template <int D>
-__global__ void __launch_bounds__(kFluxBlock)
-    flux_kernel(DevParams P, const double* __restrict__ FS, Geom g, double* __restrict__ FR) {
+__device__ __forceinline__ void flux_pass(const DevParams& P, const double* __restrict__ FS, const Geom& g,
+                                          double* __restrict__ FR) {
   const int axis = blockIdx.y;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,6 +159,22 @@ __global__ void __launch_bounds__(kFluxBlock)
     if (axis == 2)
       for (long long t = t0; t < iface_count<2>(g); t += stride) flux_elem<D, 2>(P.G, P.rp, FS, g, FR, t);
   }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kFluxBlock)
+    flux_kernel(DevParams P, const double* __restrict__ FS, Geom g, double* __restrict__ FR) {
+  flux_pass<D>(P, FS, g, FR);
+}
+
+// The 3-D pass with at least 3 CTAs per SM (<= 168 registers, some spilled):
+// the FP64 pipe needs the warps to hide its latency more than the solver
+// needs the registers (at 216 registers and 2 CTAs per SM the 256^3 step
+// was 5 % slower). In 1-D and 2-D the unbounded kernel is the faster one.
+template <int D>
+__global__ void __launch_bounds__(kFluxBlock, 3)
+    flux_kernel_3cta(DevParams P, const double* __restrict__ FS, Geom g, double* __restrict__ FR) {
+  flux_pass<D>(P, FS, g, FR);
 }
 
 // Pass 3: U^{n+1} of every interior cell, written to the other buffer.
@@ -194,7 +210,10 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
   faces_kernel<D><<<gf, kFaceBlock, 0, st>>>(P, rules_of(P), U, g, dx, s.dt, s.faces);
   if (ev) cudaEventRecord(ev[1], st);
   dim3 gr(grid_for(tot_r, kFluxBlock), D);
-  flux_kernel<D><<<gr, kFluxBlock, 0, st>>>(P, s.faces, g, s.fluxes);
+  if constexpr (D == 3)
+    flux_kernel_3cta<D><<<gr, kFluxBlock, 0, st>>>(P, s.faces, g, s.fluxes);
+  else
+    flux_kernel<D><<<gr, kFluxBlock, 0, st>>>(P, s.faces, g, s.fluxes);
   if (ev) cudaEventRecord(ev[2], st);
   const long long tot_u = (long long)g.n[0] * g.n[1] * g.n[2];
   update_kernel<D><<<grid_for(tot_u, kUpdBlock), kUpdBlock, 0, st>>>(P, U, s.fluxes, g, dx, s.dt,
