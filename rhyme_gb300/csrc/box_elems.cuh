@@ -191,7 +191,7 @@ __device__ __forceinline__ void flux_elem(const Gas<double>& G, const Rp<double>
     l[c] = ur[(long long)c * F + o];
     r[c] = ul[(long long)c * F + o + sa];
   }
-  interface_flux<D, AX>(G, rp, l, r, f);
+  interface_flux<D, AX, double, true>(G, rp, l, r, f);
 #pragma unroll
   for (int c = 0; c < D + 2; ++c) fr[(long long)c * F + o] = f[c];
 }

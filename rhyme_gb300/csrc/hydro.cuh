@@ -207,9 +207,12 @@ __device__ __forceinline__ void face_states(const Gas<T>& G, int lim, T w, const
 // Loop-invariant terms of rhyme_irs_nonlinear_wave_function.f90:15-23 for one
 // side (Ak, Bk, 2cs/gm1, 1/(rho cs)): the reference recomputes them every
 // Newton iteration with the same operations, so computing them once gives the
-// same values. In double the pair a branch needs is formed on its first use
-// (a side usually stays a shock or a rarefaction through the iteration, and
-// FP64 divisions are scarce on GB300); in float all four up front.
+// same values. With LAZY (double only) the pair a branch needs is formed on
+// its first use (a side usually stays a shock or a rarefaction through the
+// iteration, and FP64 divisions are scarce on GB300): the plain FP64 flux
+// kernels take it (2-D slab 117 -> 126 M cell-updates/s); the FP64 fix-up of
+// the mixed form does not (its kernel would spill, and the mixed batch and
+// the server's latency suffered); float forms all four up front.
 template <typename T>
 struct WaveSide {
   T rho, p, cs, Ak, Bk, c2g, irc;
@@ -230,14 +233,14 @@ __device__ __forceinline__ void wave_fan_terms(const Gas<T>& G, WaveSide<T>& w) 
   w.fan_ready = true;
 }
 
-template <typename T>
+template <typename T, bool LAZY>
 __device__ __forceinline__ WaveSide<T> wave_side(const Gas<T>& G, T s_rho, T s_p, T s_cs) {
   WaveSide<T> w;
   w.rho = s_rho;
   w.p = s_p;
   w.cs = s_cs;
   w.shock_ready = w.fan_ready = false;
-  if constexpr (sizeof(T) == sizeof(float)) {
+  if constexpr (!LAZY) {
     wave_shock_terms(G, w);
     wave_fan_terms(G, w);
   }
@@ -245,10 +248,10 @@ __device__ __forceinline__ WaveSide<T> wave_side(const Gas<T>& G, T s_rho, T s_p
 }
 
 // rhyme_irs_nonlinear_wave_function.f90:13-24
-template <typename T>
+template <typename T, bool LAZY>
 __device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, WaveSide<T>& w, T p, T& f, T& fprime) {
   if (p > w.p) {
-    if constexpr (sizeof(T) == sizeof(double)) {
+    if constexpr (LAZY) {
       if (!w.shock_ready) wave_shock_terms(G, w);
     }
     const T bp = w.Bk + p;
@@ -264,7 +267,9 @@ __device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, WaveSide<T>& w, 
     f = w.c2g * expm1f(G.gm1_2g * t);
     fprime = w.irc * expf(-G.gp1_2g * t);
   } else {
-    if (!w.fan_ready) wave_fan_terms(G, w);
+    if constexpr (LAZY) {
+      if (!w.fan_ready) wave_fan_terms(G, w);
+    }
     T y, z;
     m_pow2(p / w.p, G.gm1_2g, -G.gp1_2g, y, z);
     f = w.c2g * (y - T(1));
@@ -320,20 +325,20 @@ __device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T 
 // wave functions at the last iterate before the final update. `converged`
 // (optional) tells whether the first guess met the tolerance within the
 // iteration cap.
-template <typename T>
+template <typename T, bool LAZY>
 __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
                                       T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f,
                                       bool* converged = nullptr) {
   T p_star = T(0), p_prev, l_fp, r_fp;
   if (converged) *converged = false;
-  WaveSide<T> WL = wave_side(G, l_rho, l_p, l_cs);
-  WaveSide<T> WR = wave_side(G, r_rho, r_p, r_cs);
+  WaveSide<T> WL = wave_side<T, LAZY>(G, l_rho, l_p, l_cs);
+  WaveSide<T> WR = wave_side<T, LAZY>(G, r_rho, r_p, r_cs);
   for (int gid = 0; gid < 6; ++gid) {
     p_star = guess_p_star(G, gid, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
     p_prev = p_star;
     for (int i = 1; i <= n_iter; ++i) {
-      nonlinear_wave(G, WL, p_star, l_f, l_fp);
-      nonlinear_wave(G, WR, p_star, r_f, r_fp);
+      nonlinear_wave<T, LAZY>(G, WL, p_star, l_f, l_fp);
+      nonlinear_wave<T, LAZY>(G, WR, p_star, r_f, r_fp);
       p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
       if (p_star < T(0)) break;
       if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) {
@@ -369,10 +374,10 @@ struct Star {
 // sampling reads is formed: p* and u* (:12-38), then the left (:40, 43-53)
 // or the right (:41, 55-65) star state, each with the reference's
 // operations.
-template <int D, int AX, typename T>
+template <int D, int AX, typename T, bool LAZY>
 __device__ __forceinline__ void rp_star_pu(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
                                            const Side<D, T>& R, Star<T>& s) {
-  s.p = irs_exec(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
+  s.p = irs_exec<T, LAZY>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
                  s.r_f, &s.converged);
   if (s.p < rp.vac_p) s.p = rp.vac_p;
   s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
@@ -494,7 +499,7 @@ __device__ __forceinline__ void vacuum_state(const Gas<T>& G, const Rp<T>& rp, T
 // a vacuum or vacuum-generation branch, an interface within 10% of vacuum
 // generation or with a density or pressure ratio beyond 1e6, a first guess
 // whose Newton iteration missed the tolerance, or a non-finite state.
-template <int D, int AX, typename T, bool CHECK = false>
+template <int D, int AX, typename T, bool CHECK = false, bool LAZY = false>
 __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
                                          T dxdt, T* u, bool* need64 = nullptr) {
   Side<D, T> L, R;
@@ -572,7 +577,7 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       }
     } else {
       Star<T> s;
-      rp_star_pu<D, AX>(G, rp, L, R, s);
+      rp_star_pu<D, AX, T, LAZY>(G, rp, L, R, s);
       if (CHECK && !s.converged) {
         *need64 = true;
         return;
@@ -584,11 +589,12 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
 
 // Interface flux: Riemann state at x/t = 0 (dx = 0 in
 // rhyme_muscl_hancock_solve_memory_intensive.f90:110-116), then calc_flux.
-template <int D, int AX, typename T>
+// LAZY: see WaveSide.
+template <int D, int AX, typename T, bool LAZY = false>
 __device__ __forceinline__ void interface_flux(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
                                                T* f) {
   T u[D + 2];
-  rp_solve<D, AX>(G, rp, l, r, T(0), u);
+  rp_solve<D, AX, T, false, LAZY>(G, rp, l, r, T(0), u);
   flux<D, AX>(G, u, f);
 }
 

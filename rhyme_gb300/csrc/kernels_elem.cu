@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kBlock)
        i += (long long)gridDim.x * blockDim.x) {
     const double* q = s + i * 8;
     double lf = 0.0, rf = 0.0;
-    const double p = irs_exec(P.G, P.rp.tol, P.rp.n_iter, q[0], q[1], q[2], q[3], lf, q[4], q[5],
+    const double p = irs_exec<double, false>(P.G, P.rp.tol, P.rp.n_iter, q[0], q[1], q[2], q[3], lf, q[4], q[5],
                               q[6], q[7], rf);
     out[i * 3 + 0] = p;
     out[i * 3 + 1] = lf;
