@@ -304,6 +304,9 @@ def run_gpu(args, rank, local, world):
     K, W = args.steps, args.warmup
     compare = prec == "mixed" and not args.no_compare
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    # the host array of the end-to-end loop, allocated (and first touched)
+    # before the other runs, as a caller's state array would be
+    host = cells.copy()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -371,7 +374,6 @@ def run_gpu(args, rank, local, world):
     ctx.close()
 
     # end to end through the C-ABI with the state in host memory
-    host = cells.copy()
     ctx2 = gpu.Context(p)
     b2 = ctx2.register_box(host)
     # the drop-in mode: each solve copies its result back while it runs
