@@ -49,9 +49,12 @@ enum {
 /* Slope limiter ids: slid, rhyme_slope_limiter.f90:6-10. */
 enum { RHYME_GPU_VAN_LEER = 1, RHYME_GPU_MINMOD = 2, RHYME_GPU_VAN_ALBADA = 3,
        RHYME_GPU_SUPERBEE = 4 };
-/* Boundary ids: bcid, rhyme_samr_bc.f90:9-12. */
+/* Boundary ids: bcid, rhyme_samr_bc.f90:9-12. RHYME_GPU_HALO (no reference
+ * counterpart) leaves the face to the caller: the face of a slab of a box
+ * decomposed along its outermost axis, whose two ghost rows the caller
+ * copies from the neighbouring slab (rhyme_gpu_get_rows / _set_rows). */
 enum { RHYME_GPU_REFLECTIVE = 1, RHYME_GPU_OUTFLOW = 2, RHYME_GPU_PERIODIC = 3,
-       RHYME_GPU_INFLOW = 4 };
+       RHYME_GPU_INFLOW = 4, RHYME_GPU_HALO = 5 };
 /* Solver ids: mhid, rhyme_muscl_hancock.f90:10-15. */
 enum { RHYME_GPU_CPU_INTENSIVE = 1, RHYME_GPU_MEMORY_INTENSIVE = 2 };
 /* Arithmetic of the step (this library): FP64 throughout, or FP32
@@ -152,6 +155,23 @@ int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle);
  * rhyme_gpu_sync_to_host or rhyme_gpu_synchronize returns.
  */
 int rhyme_gpu_set_host_writeback(rhyme_gpu_ctx* ctx, int handle, int on);
+
+/*
+ * Rows [row0, row0 + nrows) of the box's outermost axis (rows of the
+ * ghosted block: 0 and 1 are the left ghosts, 2 .. N+1 the interior) of the
+ * hydro components, device -> host into out: NDIM+2 component blocks of
+ * nrows rows each, a row being the ghosted extent of the other axes. Waits.
+ * With rhyme_gpu_set_rows, the halo exchange of a box decomposed into slabs
+ * along its outermost axis (one slab per GPU): each slab sends its first and
+ * last two interior rows to the neighbours' ghost rows, whose faces have the
+ * RHYME_GPU_HALO boundary type, after the ghost fill and before the solve;
+ * dt is the minimum of the slabs' dt, which equals the whole box's dt since
+ * dt = RN(courant minval(dx) / max) is monotone in the maximum. No reference
+ * counterpart (the reference steps one box per process).
+ */
+int rhyme_gpu_get_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, double* out);
+/* The same rows host -> device, into both state buffers of the box. */
+int rhyme_gpu_set_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, const double* in);
 
 /*
  * Reads and clears the box's status word (no reference counterpart: the

@@ -172,7 +172,7 @@ int validate(rhyme_gpu_ctx* ctx, const rhyme_gpu_params* p) {
   if (!(p->kb_amu > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "kb_amu must be positive");
   if (!(p->courant > 0.0)) return fail(ctx, RHYME_GPU_EINVAL, "courant number must be positive");
   for (int i = 0; i < 2 * p->ndim; ++i)
-    if (p->bc[i] < 1 || p->bc[i] > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d on side %d", p->bc[i], i + 1);
+    if (p->bc[i] < 1 || p->bc[i] > 5) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d on side %d", p->bc[i], i + 1);
   return RHYME_GPU_OK;
 }
 
@@ -555,6 +555,54 @@ int rhyme_gpu_sync_to_host(rhyme_gpu_ctx* ctx, int handle) {
   // with write-back the solve's copies are in flight (the stream waits for them)
   if (!b->wb_pending)
     CK(cudaMemcpyAsync(b->host, b->state[b->cur], b->hydro_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return wait_stream(ctx);
+}
+
+namespace {
+
+// Checks a row range of the box's outermost axis; the copy's geometry.
+int rows_geometry(rhyme_gpu_ctx* ctx, Box* b, int row0, int nrows, long long* row, size_t* pitch) {
+  const int D = ctx->params.ndim;
+  const int rows = b->g.n[D - 1] + 4;
+  if (row0 < 0 || nrows < 1 || row0 + nrows > rows)
+    return fail(ctx, RHYME_GPU_EINVAL, "rows [%d, %d) outside 0..%d", row0, row0 + nrows, rows);
+  *row = b->g.s[D - 1];
+  *pitch = (size_t)b->g.field * sizeof(double);
+  return RHYME_GPU_OK;
+}
+
+}  // namespace
+
+int rhyme_gpu_get_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, double* out) {
+  if (!ctx || !out) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  long long row;
+  size_t pitch;
+  int rc = rows_geometry(ctx, b, row0, nrows, &row, &pitch);
+  if (rc != RHYME_GPU_OK) return rc;
+  const size_t width = (size_t)nrows * row * sizeof(double);
+  CK(cudaMemcpy2DAsync(out, width, b->state[b->cur] + (size_t)row0 * row, pitch, width, ctx->params.ndim + 2,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  return wait_stream(ctx);
+}
+
+int rhyme_gpu_set_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, const double* in) {
+  if (!ctx || !in) return fail(ctx, RHYME_GPU_EINVAL, "null argument");
+  Box* b = find_box(ctx, handle);
+  if (!b) return fail(ctx, RHYME_GPU_ENOTFOUND, "unknown box handle %d", handle);
+  long long row;
+  size_t pitch;
+  int rc = rows_geometry(ctx, b, row0, nrows, &row, &pitch);
+  if (rc != RHYME_GPU_OK) return rc;
+  const size_t width = (size_t)nrows * row * sizeof(double);
+  const size_t off = (size_t)row0 * row;
+  state_changed(b);
+  CK(cudaMemcpy2DAsync(b->state[b->cur] + off, pitch, in, width, width, ctx->params.ndim + 2,
+                       cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpy2DAsync(b->state[1 - b->cur] + off, pitch, b->state[b->cur] + off, pitch, width,
+                       ctx->params.ndim + 2, cudaMemcpyDeviceToDevice, ctx->stream));
+  // the caller's buffer may be reused on return
   return wait_stream(ctx);
 }
 
@@ -1365,7 +1413,7 @@ extern "C" int rhyme_gpu_set_box_params(rhyme_gpu_ctx* ctx, int handle, const in
   if (limiter < 1 || limiter > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown slope limiter %d", limiter);
   if (bc)
     for (int i = 0; i < 2 * D; ++i)
-      if (bc[i] < 1 || bc[i] > 4) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d", bc[i]);
+      if (bc[i] < 1 || bc[i] > 5) return fail(ctx, RHYME_GPU_EINVAL, "unknown boundary type %d", bc[i]);
   if (bc)
     for (int i = 0; i < 2 * D; ++i) b->dp.bc[i] = bc[i];
   b->dp.limiter = limiter;

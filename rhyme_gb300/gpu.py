@@ -28,6 +28,7 @@ _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMED
 EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rhyme_gpu_last_error",
            "rhyme_gpu_get_stream", "rhyme_gpu_register_box", "rhyme_gpu_unregister_box",
            "rhyme_gpu_sync_to_device", "rhyme_gpu_sync_to_host", "rhyme_gpu_set_host_writeback",
+           "rhyme_gpu_get_rows", "rhyme_gpu_set_rows",
            "rhyme_gpu_cfl_time_step", "rhyme_gpu_cfl_dt",
            "rhyme_gpu_set_boundaries", "rhyme_gpu_mh_solve", "rhyme_gpu_run", "rhyme_gpu_synchronize",
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
@@ -143,6 +144,8 @@ def load():
     L.rhyme_gpu_sync_to_device.argtypes = [vp, C.c_int]
     L.rhyme_gpu_sync_to_host.argtypes = [vp, C.c_int]
     L.rhyme_gpu_set_host_writeback.argtypes = [vp, C.c_int, C.c_int]
+    L.rhyme_gpu_get_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
+    L.rhyme_gpu_set_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
     L.rhyme_gpu_cfl_time_step.argtypes = [vp, C.c_int, dp, dp]
     L.rhyme_gpu_set_boundaries.argtypes = [vp, C.c_int]
     L.rhyme_gpu_cfl_dt.argtypes = [vp, C.c_int, dp]
@@ -303,6 +306,19 @@ class Context:
 
     def sync_to_host(self, box):
         self._check(self.lib.rhyme_gpu_sync_to_host(self.h, box.handle))
+
+    def get_rows(self, box, row0, nrows):
+        """Rows [row0, row0 + nrows) of the outermost axis of the box's
+        ghosted block, shape (NDIM+2, nrows, ...)."""
+        shape = (self.ndim + 2, int(nrows)) + box.cells.shape[2:]
+        out = np.empty(shape, dtype=np.float64)
+        self._check(self.lib.rhyme_gpu_get_rows(self.h, box.handle, int(row0), int(nrows), _d(out)))
+        return out
+
+    def set_rows(self, box, row0, rows):
+        """Writes rows (as from get_rows) at row0 into both state buffers."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        self._check(self.lib.rhyme_gpu_set_rows(self.h, box.handle, int(row0), int(rows.shape[1]), _d(rows)))
 
     def set_host_writeback(self, box, on=True):
         """Each solve of the box also copies the new state into its cells

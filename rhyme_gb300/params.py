@@ -16,6 +16,8 @@ LIMITERS = {"van_leer": VAN_LEER, "minmod": MINMOD, "van_albada": VAN_ALBADA,
             "superbee": SUPERBEE}
 # bcid
 REFLECTIVE, OUTFLOW, PERIODIC, INFLOW = 1, 2, 3, 4
+# a face whose ghost rows the caller fills (a slab of a decomposed box)
+HALO = 5
 BCS = {"reflective": REFLECTIVE, "outflow": OUTFLOW, "periodic": PERIODIC,
        "inflow": INFLOW}
 # mhid

@@ -62,3 +62,6 @@ def test_null_arguments(lib):
     assert lib.rhyme_gpu_create(None, None) == gpu.EINVAL
     assert lib.rhyme_gpu_synchronize(None) == gpu.EINVAL
     assert lib.rhyme_gpu_last_error(None) == b""
+    assert lib.rhyme_gpu_get_rows(None, 0, 0, 1, None) == gpu.EINVAL
+    assert lib.rhyme_gpu_set_rows(None, 0, 0, 1, None) == gpu.EINVAL
+    assert lib.rhyme_gpu_set_host_writeback(None, 0, 1) == gpu.EINVAL

@@ -1,0 +1,59 @@
+"""One box decomposed into slabs along its outermost axis on the GPU: the
+slabs are boxes of one context, their halo faces of type HALO filled by
+rhyme_gpu_get_rows / rhyme_gpu_set_rows, dt the minimum of the slabs' dt
+(rhyme_gb300.slabs.run_local). The slabs' interior rows and every dt equal
+the whole box's, bit for bit, in plain FP64 and in mixed precision (none of
+these steps sends an interface to the FP64 fallback, whose atomics could
+add two corrections of a cell in either order)."""
+import numpy as np
+import pytest
+
+from rhyme_gb300 import gpu, ic, slabs
+from rhyme_gb300.params import FP64, MIXED, OUTFLOW, PERIODIC
+
+pytestmark = pytest.mark.gpu
+
+
+def whole(cells, dx, p, nsteps):
+    c = cells.copy()
+    with gpu.Context(p) as ctx:
+        b = ctx.register_box(c)
+        dts = []
+        for _ in range(nsteps):
+            dt = ctx.cfl_time_step(b, dx)
+            ctx.set_boundaries(b)
+            ctx.muscl_hancock_solve(b, dx, dt)
+            dts.append(dt)
+        fb = ctx.fallback_count(b) if p["precision"] == MIXED else 0
+        ctx.sync_to_host(b)
+    return c, np.array(dts), fb
+
+
+def decomposed(cells, dx, p, nsteps, parts):
+    nz = cells.shape[1] - 4
+    rows = slabs.split_rows(nz, parts)
+    arrays = [slabs.slab_cells(cells, a, c) for a, c in rows]
+    periodic = p["bc"][4] == PERIODIC and p["bc"][5] == PERIODIC
+    with gpu.Context(p) as ctx:
+        ss = []
+        for r, arr in enumerate(arrays):
+            b = ctx.register_box(arr)
+            ctx.set_box_params(b, bc=slabs.slab_bc(p["bc"], 3, r, parts), limiter=p["limiter"], omega=p["omega"])
+            ss.append((ctx, b))
+        dts = slabs.run_local(ss, [c for _, c in rows], nsteps, slabs.GpuOps(dx), periodic)
+        fb = sum(ctx.fallback_count(b) for _, b in ss) if p["precision"] == MIXED else 0
+        for _, b in ss:
+            ctx.sync_to_host(b)
+    return rows, arrays, dts, fb
+
+
+@pytest.mark.parametrize("precision,parts,bc_z", [(MIXED, 3, PERIODIC), (FP64, 2, PERIODIC), (MIXED, 4, OUTFLOW)])
+def test_slabs_equal_whole_box(precision, parts, bc_z):
+    cells, dx, p = ic.spheres_3d(n=48, nspheres=6, seed=4)
+    p = dict(p, precision=precision, bc=[PERIODIC] * 4 + [bc_z, bc_z])
+    ref, dref, fa = whole(cells, dx, p, 8)
+    rows, arrays, d, fb = decomposed(cells, dx, p, 8, parts)
+    assert fa == 0 and fb == 0
+    assert np.array_equal(d, dref)
+    for (a, c), arr in zip(rows, arrays):
+        assert np.array_equal(arr[:, 2:2 + c], ref[:, 2 + a:2 + a + c])
