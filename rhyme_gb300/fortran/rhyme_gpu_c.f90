@@ -21,6 +21,9 @@ module rhyme_gpu_c
    integer(c_int), parameter :: rhyme_gpu_mixed = 1
    integer(c_int), parameter :: rhyme_gpu_tune_auto = 0
    integer(c_int), parameter :: rhyme_gpu_tune_fixed = 1
+   ! boundary type of a face whose ghost rows the caller fills (a slab of a
+   ! box decomposed over several GPUs); the others are bcid's values
+   integer(c_int), parameter :: rhyme_gpu_halo = 5
 
    type, bind(c) :: rhyme_gpu_params_t
       integer(c_int) :: ndim = 0
@@ -94,6 +97,22 @@ module rhyme_gpu_c
          type(c_ptr), value :: ctx
          integer(c_int), value :: handle, on
       end function rhyme_gpu_set_host_writeback
+
+      ! rows row0 .. row0+nrows-1 (0-based, ghost rows included) of the
+      ! outermost axis of the hydro components: the halo of a slab
+      integer(c_int) function rhyme_gpu_get_rows(ctx, handle, row0, nrows, rows) bind(c, name='rhyme_gpu_get_rows')
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: handle, row0, nrows
+         real(c_double), intent(out) :: rows(*)
+      end function rhyme_gpu_get_rows
+
+      integer(c_int) function rhyme_gpu_set_rows(ctx, handle, row0, nrows, rows) bind(c, name='rhyme_gpu_set_rows')
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: handle, row0, nrows
+         real(c_double), intent(in) :: rows(*)
+      end function rhyme_gpu_set_rows
 
       integer(c_int) function rhyme_gpu_box_status(ctx, handle, flags) bind(c, name='rhyme_gpu_box_status')
          import :: c_int, c_ptr
