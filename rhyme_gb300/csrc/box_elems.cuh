@@ -52,9 +52,13 @@ __host__ __device__ inline void ghost_offsets(const Geom& g, long long& off1, lo
 // K1 element: fills the left then the right 2-cell ghost layer of one line
 // (axis, component, transverse position) in the order of
 // rhyme_samr_bc_set_boundaries.f90:9-20; writes U and (if given) M.
+// M (optional) receives the same ghost values (the other state buffer); Mf
+// (optional) their FP32 images (the mirror of the mixed form), equal to what
+// a fill of the mirror from its own interior would write.
 template <int D, typename T>
 __device__ __forceinline__ void ghost_elem(const BoxRules& R, T* __restrict__ U, T* __restrict__ M,
-                                           const Geom& g, long long off1, long long off2, long long t) {
+                                           const Geom& g, long long off1, long long off2, long long t,
+                                           float* __restrict__ Mf = nullptr) {
   int axis;
   long long r;
   if (t < off1) {
@@ -113,6 +117,11 @@ __device__ __forceinline__ void ghost_elem(const BoxRules& R, T* __restrict__ U,
       T* m = M + (long long)c * g.field;
       m[g0] = f[g0];
       m[g1] = f[g1];
+    }
+    if (Mf) {
+      float* m = Mf + (long long)c * g.field;
+      m[g0] = (float)f[g0];
+      m[g1] = (float)f[g1];
     }
   }
 }

@@ -46,10 +46,10 @@ inline int grid_for(long long total, int block) {
 template <int D, typename T>
 __global__ void __launch_bounds__(kFillBlock)
     ghost_fill_kernel(BoxRules R, T* __restrict__ U, T* __restrict__ M, Geom g, long long off1,
-                      long long off2, long long total) {
+                      long long off2, long long total, float* __restrict__ Mf) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x)
-    ghost_elem<D, T>(R, U, M, g, off1, off2, t);
+    ghost_elem<D, T>(R, U, M, g, off1, off2, t, Mf);
 }
 
 // ------------------------------------------------------------------ K2 ---
@@ -227,28 +227,29 @@ cudaError_t mh_solve_d(const DevParams& P, const double* U, double* Unew, const 
 int max_cfl_blocks() { return kMaxBlocks; }
 
 template <int D, typename T>
-cudaError_t ghost_fill_d(const BoxRules& R, T* U, T* U_mirror, const Geom& g, cudaStream_t st) {
+cudaError_t ghost_fill_d(const BoxRules& R, T* U, T* U_mirror, const Geom& g, cudaStream_t st, float* Uf) {
   long long off1, off2, total;
   ghost_offsets<D>(g, off1, off2, total);
   ghost_fill_kernel<D, T><<<grid_for(total, kFillBlock), kFillBlock, 0, st>>>(R, U, U_mirror, g, off1, off2,
-                                                                              total);
+                                                                              total, Uf);
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t ghost_fill_any(const DevParams& P, T* U, T* U_mirror, const Geom& g, cudaStream_t st) {
+cudaError_t ghost_fill_any(const DevParams& P, T* U, T* U_mirror, const Geom& g, cudaStream_t st,
+                           float* Uf = nullptr) {
   const BoxRules R = rules_of(P);
   switch (P.ndim) {
-    case 1: return ghost_fill_d<1, T>(R, U, U_mirror, g, st);
-    case 2: return ghost_fill_d<2, T>(R, U, U_mirror, g, st);
-    case 3: return ghost_fill_d<3, T>(R, U, U_mirror, g, st);
+    case 1: return ghost_fill_d<1, T>(R, U, U_mirror, g, st, Uf);
+    case 2: return ghost_fill_d<2, T>(R, U, U_mirror, g, st, Uf);
+    case 3: return ghost_fill_d<3, T>(R, U, U_mirror, g, st, Uf);
   }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,
-                              cudaStream_t st) {
-  return ghost_fill_any<double>(P, U, U_mirror, g, st);
+                              cudaStream_t st, float* Uf) {
+  return ghost_fill_any<double>(P, U, U_mirror, g, st, Uf);
 }
 
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st) {

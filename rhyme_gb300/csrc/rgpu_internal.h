@@ -137,8 +137,10 @@ struct Dx {
 };
 
 // Launchers (kernels_box.cu). All asynchronous on `st`.
+// Ghost fill of U, its values also written to U_mirror (the other state
+// buffer) and, as FP32, to Uf (the mixed form's mirror) when given.
 cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,
-                              cudaStream_t st);
+                              cudaStream_t st, float* Uf = nullptr);
 cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const Dx& dx,
                        const StepScratch& s, cudaStream_t st);
 // ev (optional, 4 events): recorded before the face pass and after the face,
