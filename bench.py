@@ -227,8 +227,8 @@ def allsum(x, world):
 def launches_per_step(prec, ndim):
     """Kernels of this library launched per single-box step: FP64 cfl, ghost
     fill, faces, fluxes, update; mixed cfl (which also writes the FP32
-    mirror), ghost fill (of the FP64 state and of the mirror, in one kernel
-    beside the cfl), one sweep per axis and the FP64 fix-up of the queued
+    mirror), ghost fill (of the FP64 state and of the mirror, in one
+    kernel), one sweep per axis and the FP64 fix-up of the queued
     interfaces."""
     return 5 if prec == "fp64" else 3 + ndim
 
