@@ -2,6 +2,7 @@
 (detmath.h), computed with mpmath at 200 bits.
 
     python rhyme_gb300/csrc/detmath_tables.py   # rewrites detmath_tables.h
+    python rhyme_gb300/csrc/detmath_tables.py OUT  # writes OUT instead
 
 log: for m in [1, 2) the interval i = floor((m - 1) 128) has centre
 c_i = 1 + (i + 1/2)/128; INVC[i] = RN(1/c_i) and LOGC[i] = -log(INVC[i]) as a
@@ -28,7 +29,7 @@ def fmt(x):
     return repr(float(x)) if x != 0 else "0.0"
 
 
-def main():
+def main(out=None):
     lines = ["// detmath_tables.h -- constants of det_pow (detmath.h), written by",
              "// detmath_tables.py (mpmath, 200 bits); do not edit by hand.",
              "#pragma once", "",
@@ -68,11 +69,13 @@ def main():
     for k in range(len(lines)):
         if lines[k].startswith("#define DETMATH_") or (lines[k].startswith("    ") and k + 1 < len(lines)):
             lines[k] += " \\"
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "detmath_tables.h")
+    if out is None:
+        out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "detmath_tables.h")
     with open(out, "w") as f:
         f.write("\n".join(lines))
     print("wrote", out)
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

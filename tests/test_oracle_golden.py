@@ -249,6 +249,19 @@ def test_det_pow_correctly_rounded():
         assert np.all(np.abs(det.view(np.int64) - exact.view(np.int64)) <= 1)
 
 
+def test_detmath_tables_regenerate(tmp_path):
+    """The committed power-function tables are what their generator writes."""
+    pytest.importorskip("mpmath")
+    import importlib.util
+    here = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "rhyme_gb300", "csrc")
+    spec = importlib.util.spec_from_file_location("detmath_tables", os.path.join(here, "detmath_tables.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    out = tmp_path / "detmath_tables.h"
+    mod.main(str(out))
+    assert out.read_text() == open(os.path.join(here, "detmath_tables.h")).read()
+
+
 def test_det_mode_matches_libm_mode_closely(golden_dir):
     """The oracle's det_pow mode passes the same golden p* rows and stays
     within 1e-13 of the libm mode."""
