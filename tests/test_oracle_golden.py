@@ -2,7 +2,7 @@
 
 Each test restates one of Rhyme's unit tests for the hot path, with the same
 inputs and the same tolerance semantics (tests/refcheck.py), so the oracle
-is shown to reproduce the reference before it is used to judge the GPU.
+is shown to reproduce the reference before it checks the GPU.
 """
 import json
 import os
