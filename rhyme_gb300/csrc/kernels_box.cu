@@ -256,6 +256,15 @@ cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, 
   return ghost_fill_any<float>(P, Uf, nullptr, g, st);
 }
 
+namespace {
+__global__ void set_double_kernel(double* dst, double v) { *dst = v; }
+}  // namespace
+
+cudaError_t launch_set_double(double* dst, double v, cudaStream_t st) {
+  set_double_kernel<<<1, 1, 0, st>>>(dst, v);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cfl(const DevParams& P, const double* U, const Geom& g, const Dx& dx,
                        const StepScratch& s, cudaStream_t st) {
   const long long total = (long long)g.n[0] * g.n[1] * g.n[2];

@@ -34,8 +34,6 @@ double* g_scratch_addr[kMaxDevices] = {};
 std::once_flag g_scratch_once[kMaxDevices];
 cudaError_t g_scratch_err[kMaxDevices] = {};
 
-__global__ void set_dt_kernel(double* p, double v) { *p = v; }
-
 // Device address of the scratch array on `dev` (the current device), looked
 // up once per device.
 cudaError_t scratch_on(int dev, double** out) {
@@ -129,8 +127,7 @@ extern "C" int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params, const 
   s.faces = base + 32;
   s.fluxes = s.faces + 2LL * D * (D + 2) * g.field;
   cudaStream_t st = (cudaStream_t)stream;
-  set_dt_kernel<<<1, 1, 0, st>>>(s.dt, dt);
-  e = cudaGetLastError();
+  e = launch_set_double(s.dt, dt, st);
   if (e == cudaSuccess) e = launch_mh_solve(P, d_cells_in, d_cells_out, g, d, s, st);
   if (e != cudaSuccess) {
     fprintf(stderr, "rhyme_gpu_mh_solve_noalloc: %s\n", cudaGetErrorString(e));

@@ -137,6 +137,8 @@ struct Dx {
 };
 
 // Launchers (kernels_box.cu). All asynchronous on `st`.
+// *dst = v in stream order (a scalar from the host without a staging buffer).
+cudaError_t launch_set_double(double* dst, double v, cudaStream_t st);
 // Ghost fill of U, its values also written to U_mirror (the other state
 // buffer) and, as FP32, to Uf (the mixed form's mirror) when given.
 cudaError_t launch_ghost_fill(const DevParams& P, double* U, double* U_mirror, const Geom& g,

@@ -82,7 +82,7 @@ struct rhyme_gpu_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   std::vector<Box*> boxes;
-  double* pinned_dt = nullptr;   // pinned host scalar for dt up/down loads
+  double* pinned_dt = nullptr;   // pinned host scalars read back synchronously (dt, status, totals)
   void* elem_buf = nullptr;      // growable device buffer for element calls
   size_t elem_cap = 0;
   double timeout_s = 600.0;
@@ -887,12 +887,10 @@ int rhyme_gpu_mh_solve(rhyme_gpu_ctx* ctx, int handle, const double dx[3], doubl
   Dx d = make_dx(ctx->params.ndim, dx);
   int rc = box_plan(ctx, b, d);
   if (rc != RHYME_GPU_OK) return rc;
-  // The pinned staging scalar may still be read by an earlier copy; wait for
-  // it before reuse (cheap: the stream is usually idle at this point).
-  rc = wait_stream(ctx);
-  if (rc != RHYME_GPU_OK) return rc;
-  ctx->pinned_dt[0] = dt;
-  CK(cudaMemcpyAsync(b->s.dt, ctx->pinned_dt, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // dt by value through a one-thread kernel: no host staging buffer, so no
+  // wait for the stream (the host enqueues the solve while the ghost fill
+  // or an upload still runs)
+  CK(launch_set_double(b->s.dt, dt, ctx->stream));
   bool written_back = false;
   if (ctx->mixed) {
     // the FP32 mirror of the whole box (ghosts included) from the state this
