@@ -1,7 +1,8 @@
 """One box decomposed into slabs along its outermost axis (rhyme_gb300.slabs),
 on the CPU with the oracle standing in for each slab's GPU: in one process
-and as gloo ranks (world sizes 2 and 3, periodic and outflow along the axis),
-the slabs' interior rows and every dt equal the whole box's, bit for bit."""
+(1-, 2- and 3-D) and as gloo ranks (world sizes 2 and 3, periodic and
+outflow along the axis), the slabs' interior rows and every dt equal the
+whole box's, bit for bit."""
 import os
 import socket
 
@@ -92,6 +93,36 @@ def test_local_slabs_equal_whole_box(bc_z, parts):
     d = slabs.run_local(ss, [c for _, c in parts_rows], 6, OracleOps(dx), periodic=(bc_z == PERIODIC))
     assert np.array_equal(d, dref)
     for (a, c), (_, sc) in zip(parts_rows, ss):
+        assert np.array_equal(sc[:, 2:2 + c], ref[:, 2 + a:2 + a + c])
+
+
+def box_nd(ndim, bc_last, seed=2):
+    """A 1-D (40 cells) or 2-D (14 x 24) box with a seeded random state; the
+    outermost axis is the last one."""
+    dims = {1: [40], 2: [14, 24]}[ndim]
+    rng = np.random.default_rng(seed)
+    shp = tuple(dims[::-1])
+    rho = 1.0 + 0.3 * rng.random(shp)
+    vel = [0.2 * (rng.random(shp) - 0.5) for _ in range(ndim)]
+    pr = 1.0 + 0.5 * rng.random(shp)
+    cells = ic.empty_box(ndim, dims)
+    cells[ic.interior(ndim, dims)] = ic.prim_to_cons(rho, vel, pr, 5.0 / 3.0)
+    bc = [REFLECTIVE, OUTFLOW][:2 * ndim - 2] + [bc_last, bc_last]
+    p = hydro_params(ndim, limiter=SUPERBEE, bc=bc, courant=0.5)
+    return cells, [1.0 / max(dims)] * ndim, p
+
+
+@pytest.mark.parametrize("ndim,bc_last,parts", [(1, PERIODIC, 3), (1, OUTFLOW, 2), (2, PERIODIC, 3), (2, REFLECTIVE, 4)])
+def test_local_slabs_equal_whole_box_1d_2d(ndim, bc_last, parts):
+    cells, dx, p = box_nd(ndim, bc_last)
+    ref, dref = whole(cells, dx, p, 8)
+    n = cells.shape[1] - 4
+    rows = slabs.split_rows(n, parts)
+    ss = [(dict(p, bc=slabs.slab_bc(p["bc"], ndim, r, parts)), slabs.slab_cells(cells, a, c))
+          for r, (a, c) in enumerate(rows)]
+    d = slabs.run_local(ss, [c for _, c in rows], 8, OracleOps(dx), periodic=(bc_last == PERIODIC))
+    assert np.array_equal(d, dref)
+    for (a, c), (_, sc) in zip(rows, ss):
         assert np.array_equal(sc[:, 2:2 + c], ref[:, 2 + a:2 + a + c])
 
 
