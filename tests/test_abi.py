@@ -65,3 +65,43 @@ def test_null_arguments(lib):
     assert lib.rhyme_gpu_get_rows(None, 0, 0, 1, None) == gpu.EINVAL
     assert lib.rhyme_gpu_set_rows(None, 0, 0, 1, None) == gpu.EINVAL
     assert lib.rhyme_gpu_set_host_writeback(None, 0, 1) == gpu.EINVAL
+
+
+FORTRAN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "rhyme_gb300", "fortran")
+
+
+def _fortran_bindings():
+    """(C names bound in rhyme_gpu_c.f90, fields of rhyme_gpu_params_t)."""
+    import re
+    src = open(os.path.join(FORTRAN, "rhyme_gpu_c.f90")).read()
+    names = re.findall(r"bind\(c, name='(rhyme_gpu_[a-z_0-9]+)'\)", src)
+    body = src[src.index("type, bind(c) :: rhyme_gpu_params_t"):src.index("end type rhyme_gpu_params_t")]
+    fields = re.findall(r"(integer\(c_int\)|real\(c_double\)) :: (\w+)(?:\(([\d, ]+)\))?", body)
+    return names, fields
+
+
+def test_fortran_bindings_name_declared_functions():
+    """The uncompiled Fortran interfaces bind only functions the header
+    declares (and the library exports)."""
+    names, _ = _fortran_bindings()
+    assert len(names) >= 20
+    assert set(names) <= set(gpu.EXPORTS), sorted(set(names) - set(gpu.EXPORTS))
+
+
+def test_fortran_params_type_matches_the_c_struct():
+    """rhyme_gpu_params_t has the C struct's fields in order, with the same
+    kinds and element counts (Fortran inflow(5, 6) is C inflow[6][5])."""
+    _, fields = _fortran_bindings()
+    got = []
+    for kind, name, dims in fields:
+        n = 1
+        for d in (dims.split(",") if dims else []):
+            n *= int(d)
+        got.append((name, "int" if kind.startswith("integer") else "double", n))
+    want = []
+    for name, ctype in gpu.Params._fields_:
+        n = C.sizeof(ctype)
+        base = "double" if "double" in repr(ctype) else "int"
+        want.append((name, base, n // (8 if base == "double" else 4)))
+    assert got == want
+
