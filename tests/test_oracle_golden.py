@@ -89,6 +89,33 @@ def test_riemann_sampling_sod(golden_dir):
         assert within(pe / 0.4, e_int[i], 15), ("e_int", i)
 
 
+@pytest.mark.parametrize("mirror", [False, True])
+def test_rarefaction_fans_closed_form(golden_dir, mirror):
+    """rhyme_riemann_problem_w_kfan_test.f90:55-80: inside a rarefaction fan
+    the sampled state is the closed form of riemann_problem_w_kfan (cs taken
+    negative for a right fan): rho = rho_k (2/gp1 + gm1_gp1/cs (v_k - x/t))**(2/gm1),
+    v = 2/gp1 (cs + gm1/2 v_k + x/t), p = p_k (...)**(1/gm1_2g). Sod's left fan
+    spans x/t in [-1.183, -0.070]; its mirror image has a right fan on
+    [0.070, 1.183]."""
+    g = GAMMA["diatomic"]
+    gm1, gp1 = g - 1.0, g + 1.0
+    case = [c for c in _toro_cases(golden_dir) if c["name"] == "Sod"][0]
+    if mirror:
+        case = dict(case, left=case["right"], right=case["left"])
+    sides = _sides(case, g)
+    xs = np.linspace(0.2, 1.1, 10) * (1.0 if mirror else -1.0)
+    _, u = oracle.star_and_sample(g, KB_AMU_SI, 0.0, 1e-8, 1000, sides, xs, 1.0)
+    rho_k, v_k, p_k, cs_k = sides[4:8] if mirror else sides[0:4]
+    cs = -cs_k if mirror else cs_k
+    base = 2.0 / gp1 + gm1 / gp1 / cs * (v_k - xs)
+    rho = rho_k * base ** (2.0 / gm1)
+    v = 2.0 / gp1 * (cs + gm1 / 2.0 * v_k + xs)
+    p = p_k * base ** (1.0 / (gm1 / (2.0 * g)))
+    e = 0.5 * rho * v * v + p / gm1
+    for i in range(len(xs)):
+        assert within(rho[i], u[i, 0], 14) and within(rho[i] * v[i], u[i, 1], 13) and within(e[i], u[i, 2], 14), i
+
+
 def test_riemann_solve_wave_edges(golden_dir):
     """rhyme_riemann_problem_solve_test.f90:43-178: solve() sampled just
     outside / inside each wave of the five Toro problems."""
