@@ -21,11 +21,18 @@
 // (limited slopes and half-step face states of its two cells, exact Riemann
 // problem, flux: the device code of the plain path instantiated for double),
 // and applies -+ dt/dx * F to the two adjacent interior cells of U^{n+1}.
-// Keeping the FP64 code out of the sweeps keeps them at ~64 registers (it
+// Keeping the FP64 code out of the sweeps keeps them at 50-52 registers (it
 // tripled their register count inline).
 //
 // The CFL maximum of the mixed path is taken in FP32 over the mirror; dt
 // itself is formed in FP64.
+//
+// For the drop-in loop with the state in host memory, ingest_kernel takes
+// each slab of an upload as it arrives (the mirror, the ghost cells of the
+// other buffer, the slab's share of the CFL maximum), cfl_finish_kernel
+// forms dt from that maximum, and launch_mh_solve_mixed_slab solves the box
+// in slabs of rows, each with the FP64 fix-up of the entries queued so far,
+// so that finished rows can be copied back while the next slab is solved.
 #include <math_constants.h>
 
 #include "rgpu_internal.h"

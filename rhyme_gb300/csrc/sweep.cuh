@@ -18,7 +18,8 @@ namespace {
 // Threads of a tile's CTA: one per interface of the tile ((S+1)·P, the
 // costliest phase), rounded up to whole warps, so that no phase but the
 // shared-memory staging needs a second, mostly idle round behind a barrier;
-// at most 512. CTAs per SM such that a thread may keep up to 72 registers.
+// at most 512. CTAs per SM such that a thread may keep up to 56 registers
+// (4 CTAs of 288 threads: the sweeps use 50-52 without spilling).
 template <int S, int P>
 struct TileCfg {
   static constexpr int warps_ = ((S + 1) * P + 31) / 32;
