@@ -1,10 +1,15 @@
 // rhyme_gpu.cu -- host side of the C-ABI (include/rhyme_gpu.h).
 //
 // A context holds the run parameters (the values of Rhyme's solver modules),
-// one CUDA stream and a registry of boxes. Each box owns two device state
-// buffers (ping-pong: the unsplit update reads U^n and writes U^{n+1}), the
-// solver scratch, and up to two captured CUDA graphs of one driver step (one
-// per buffer parity) that rhyme_gpu_run replays.
+// one CUDA stream, a copy stream (made on first use) and a registry of
+// boxes. Each box owns two device state buffers (ping-pong: the unsplit
+// update reads U^n and writes U^{n+1}), the solver scratch, and up to two
+// captured CUDA graphs of one driver step (one per buffer parity) that
+// rhyme_gpu_run replays. Large 2-/3-D mixed boxes with a page-locked host
+// array move in slabs of rows on the copy stream, overlapped with the
+// kernels (upload_slabs, solve_slabs_write_back). Below the single-box
+// entry points: the autotuner, level output, sanity checks and painting,
+// batches, and the server.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
