@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from rhyme_gb300 import gpu, ic
-from rhyme_gb300.params import MINMOD, MIXED, OUTFLOW, hydro_params
+from rhyme_gb300.params import FP64, MINMOD, MIXED, OUTFLOW, hydro_params
 
 pytestmark = pytest.mark.gpu
 
@@ -59,6 +59,17 @@ def test_overlapped_drop_in_matches_run_3d():
     assert np.array_equal(da, db) and np.array_equal(da, dc)
     assert np.array_equal(a, b)
     assert np.array_equal(a, c)
+
+
+def test_fp64_write_back_matches_run():
+    """Plain FP64 (no slab path): the solve's write-back is one copy after it,
+    and the drop-in loop still equals the resident run bit for bit."""
+    cells, dx, p = ic.spheres_3d(n=32, nspheres=4, seed=6)
+    q = dict(p, precision=FP64)
+    a, da, _ = resident(q, cells, dx, 4)
+    b, db, _ = drop_in(q, cells, dx, 4, writeback=True)
+    assert np.array_equal(da, db)
+    assert np.array_equal(a, b)
 
 
 def test_overlapped_drop_in_matches_run_2d():
