@@ -20,7 +20,8 @@ iteration (dt -> ghost fill -> solve) over the box.
           over that kernel's event-timed duration per step.
   cpu_baseline  the CPU oracle (a restatement of the reference's
           memory-intensive solver with OpenMP over the outer loop) on a
-          bounded sample of the same workload, all host threads.
+          bounded sample of the same workload, all host threads
+          (--cpu-threads N for fewer).
 
 Other workloads (--workload): slab2d (2-D 256^2 shear slab, plain FP64,
 500 steps), riemann1d (1-D 512 cells, 100 steps), spheres3d<N>, batch4096
@@ -28,7 +29,8 @@ Other workloads (--workload): slab2d (2-D 256^2 shear slab, plain FP64,
 seeded Poisson stream of requests served by the continuous-batching server
 against one-at-a-time plain FP64).
 
---impl reference times the CPU implementation alone on the same config.
+--impl reference times the CPU implementation alone on the same config
+(with --cpu-threads N, on N OpenMP threads).
 Under torchrun each rank runs an independent replica (the path shards by
 box; a single box is replicated) and value is the sum over ranks.
 """
@@ -249,16 +251,64 @@ def reference_sample(name, cells, dx, p, cfg):
     return cells.copy(), cfg["cells"], "the whole box per step"
 
 
+REF_BATCH_BOXES = 64
+
+
+def run_reference_batch(args):
+    """The reference arm on the many-box workload: the CPU implementation
+    steps the first REF_BATCH_BOXES boxes of the same seeded list (the list
+    is drawn box by box from one generator, so these are the batch's own
+    first boxes), box after box as the reference's driver loop does, each
+    with its own dt. Boxes are independent, so the subset changes the
+    sample's size, not its work per cell."""
+    from rhyme_gb300 import ic
+    from rhyme_gb300.params import FP64
+    import oracle
+    nthreads = args.cpu_threads or os.cpu_count() or 1
+    nb = min(args.nboxes, REF_BATCH_BOXES)
+    items = ic.batch_boxes(nb, seed=0)
+    states = [c.copy() for c, _, _ in items]
+    n = sum(int(np.prod([s - 4 for s in c.shape[1:]])) for c, _, _ in items)
+
+    def steps(k):
+        for _ in range(k):
+            for st, (_, dx, p) in zip(states, items):
+                oracle.run(dict(p, precision=FP64), st, dx, 1, nthreads=nthreads)
+
+    steps(args.warmup)
+    t0 = time.perf_counter()
+    steps(args.steps)
+    t = time.perf_counter() - t0
+    v = n * args.steps / t
+    sample = ("%d timed steps after %d warm-up steps; the first %d of the %d boxes (%d cells), one box "
+              "after another; OpenMP over each box's outer cell loop" % (args.steps, args.warmup, nb,
+                                                                           args.nboxes, n))
+    cfg = {"workload": "%d uneven 3-D boxes (edges 8..64 per axis), Riemann or sphere ICs, van Albada, "
+                       "courant 0.3, plain FP64" % args.nboxes, "cells": n, "boxes": nb,
+           "l2": "the sample's state (%.2f GB of FP64) is stepped box by box" % (n * 40 / 1e9),
+           "parallelism": "one CPU process"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     from rhyme_gb300.params import FP64
-    if args.workload in ("batch4096", "serve"):
-        raise SystemExit("--impl reference covers the single-box workloads")
+    if args.workload == "serve":
+        raise SystemExit("--impl reference covers the box workloads")
+    if args.workload == "batch4096":
+        return run_reference_batch(args)
     cells, dx, p, cfg = workload(args.workload, "fp64")
     p = dict(p, precision=FP64)  # the CPU implementation is FP64
     import oracle
-    nthreads = os.cpu_count() or 1
+    nthreads = args.cpu_threads or os.cpu_count() or 1
     c, n, what = reference_sample(args.workload, cells, dx, p, cfg)
     if args.warmup:
         oracle.run(p, c, dx, args.warmup, nthreads=nthreads)
@@ -411,7 +461,7 @@ def run_gpu(args, rank, local, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        nthreads = os.cpu_count() or 1
+        nthreads = args.cpu_threads or os.cpu_count() or 1
         v, n, t = cpu_sample(cells, dx, dict(p, precision=FP64), cfg["steps_in_run"], args.cpu_budget, nthreads)
         cpu = {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
                "sample": "first %d steps of the same workload (%.1f s), CPU oracle (FP64), OpenMP" % (n, t)}
@@ -598,6 +648,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0,
+                    help="OpenMP threads of the CPU oracle legs (default: every core)")
     ap.add_argument("--nboxes", type=int, default=4096)
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--rate", type=float, default=8.0)
