@@ -97,11 +97,15 @@ def run_local(slabs, counts, nsteps, ops, periodic):
     return np.array(dts)
 
 
-def run_rank(slab, count, nsteps, ops, periodic, rank, world, device="cpu"):
+def run_rank(slab, count, nsteps, ops, periodic, rank, world, device=None):
     """nsteps steps of this rank's slab in a torch.distributed job of
-    `world` ranks (slab r on rank r); returns the dt trace."""
+    `world` ranks (slab r on rank r); returns the dt trace. The dt and the
+    halo rows travel as tensors on `device`: by default the current CUDA
+    device under NCCL (which carries only CUDA tensors), the CPU otherwise."""
     import torch
     import torch.distributed as dist
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
     dts = []
     left, right = neighbours(rank, world, periodic)
     for _ in range(nsteps):
