@@ -191,6 +191,18 @@ def test_ideal_gas_flux(ndim):
     assert within(f[ndim + 1], v[0] * (u[ndim + 1] + p), 15)
 
 
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+def test_ideal_gas_pressure_and_sound_speed(ndim):
+    """rhyme_ideal_gas_pressure_test.f90:14-20 (p of the factory's state,
+    15 s.f.) and rhyme_ideal_gas_speed_of_sound_test.f90:14-23
+    (cs = sqrt(7/5 p / rho), 15 s.f.)."""
+    u, rho, v, p, kb_amu = _hy_conserved(ndim)
+    for axis in range(ndim):
+        _, pp, cs = oracle.eos(ndim, 1.4, kb_amu, u[None, :], axis)
+        assert within(pp[0], p, 15)
+        assert within(cs[0], np.sqrt(7.0 / 5.0 * p / rho), 15)
+
+
 @pytest.mark.parametrize("limiter", [1, 2, 3, 4])
 @pytest.mark.parametrize("ndim", [1, 3])
 def test_slope_limiter_signs(limiter, ndim):
