@@ -159,6 +159,39 @@ def test_riemann_solve_wave_edges(golden_dir):
             assert within(solve(dx, dx / ST + eps), cons(star[3], u_star, p_star), 14)
 
 
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_star_states_keep_their_side_transverse_velocities(golden_dir, axis):
+    """rhyme_riemann_problem_w_star{l,r}_{sho,fan}_test.f90: a star state
+    along an axis is prim_to_cons(rho*_K, v with u* along the axis and side
+    K's transverse velocities, p*). Sampled through the 3-D solve midway in
+    each star region of Toro's five problems, with distinct transverse
+    velocities on the two sides; p*, u* and rho*_K from the 1-D star
+    routine."""
+    g = GAMMA["diatomic"]
+    p = dict(ndim=3, gamma=g, kb_amu=KB_AMU_SI, courant=0.8, limiter=2, n_iter=1000,
+             tol=1e-8, bc=[2] * 6)
+    trans = {"left": (0.3, -0.7), "right": (-1.1, 0.45)}
+    for case in _toro_cases(golden_dir):
+        star, _ = oracle.star_and_sample(g, KB_AMU_SI, 0.0, 1e-8, 1000, _sides(case, g))
+        p_star, u_star = star[0], star[1]
+        rows = {}
+        for side in ("left", "right"):
+            c = case[side]
+            v = np.zeros(3)
+            v[axis] = c["u"]
+            v[[a for a in range(3) if a != axis]] = trans[side]
+            rows[side] = np.concatenate([[c["rho"]], c["rho"] * v,
+                                         [0.5 * c["rho"] * np.dot(v, v) + c["p"] / (g - 1.0)]])[None, :]
+        for side, rho_star, x in (("left", star[3], 0.5 * (star[5] + u_star)),
+                                  ("right", star[7], 0.5 * (u_star + star[9]))):
+            got = oracle.riemann_solve(p, rows["left"], rows["right"], x, 1.0, axis)[0]
+            v = np.zeros(3)
+            v[axis] = u_star
+            v[[a for a in range(3) if a != axis]] = trans[side]
+            want = np.concatenate([[rho_star], rho_star * v, [0.5 * rho_star * np.dot(v, v) + p_star / (g - 1.0)]])
+            assert within(got, want, 13), (case["name"], side, got, want)
+
+
 def _hy_conserved(ndim):
     """rhyme_hydro_base_factory.f90:14-67 (rho 12.3, v .12/.23/.34, T 1e4,
     mu .76, gamma 1.4)."""
