@@ -105,3 +105,25 @@ def test_fortran_params_type_matches_the_c_struct():
         want.append((name, base, n // (8 if base == "double" else 4)))
     assert got == want
 
+
+
+@pytest.mark.parametrize("compiler,flags", [("gcc", ["-std=c99", "-x", "c"]),
+                                            ("g++", ["-std=c++11", "-x", "c++"])])
+def test_header_is_plain_c_and_a_c_driver_links(lib, tmp_path, compiler, flags):
+    """tests/c_abi_driver.c (the driver loop of src/main.f90:106-177 in C)
+    compiles with warnings as errors as strict C99 and as C++, and links
+    against the built library: every entry point it calls resolves."""
+    import shutil
+    import subprocess
+    if shutil.which(compiler) is None:
+        pytest.skip("%s not found" % compiler)
+    src = os.path.join(ROOT, "tests", "c_abi_driver.c")
+    obj = str(tmp_path / "driver.o")
+    cmd = [compiler] + flags + ["-Wall", "-Wextra", "-Werror", "-pedantic",
+                                "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    exe = str(tmp_path / "driver")
+    out = subprocess.run([compiler, obj, "-L", build.OUT_DIR, "-lrhyme_gpu", "-o", exe],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
