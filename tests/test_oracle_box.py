@@ -71,6 +71,31 @@ def test_set_boundaries(ndim, dims, bctype):
         assert np.array_equal(cells[:, 1, 1], before[:, 1, 1])
 
 
+@pytest.mark.parametrize("ndim,dims", [(1, [16]), (2, [16, 8]), (3, [16, 8, 4])])
+def test_set_inflow_boundaries(ndim, dims):
+    """rhyme_samr_bc_set_{left,...,front}_boundary_test.f90 (inflow): both
+    ghost layers of an inflow face hold the face's cons_inflows (rho 1.23,
+    every momentum 2.34, e_tot 3.45); here each face gets its own values
+    (offset by the face index) so that a face written from another face's
+    values would show."""
+    cells = _random_box(ndim, dims)
+    before = cells.copy()
+    inflow = [[1.23 + f, *([2.34 + f] * ndim), 3.45 + f] for f in range(6)]
+    oracle.set_boundaries(dict(_params(ndim, [4] * 6), inflow=inflow), cells)
+    for axis in range(ndim):
+        N = dims[axis]
+        for side, ghosts in ((0, (0, -1)), (1, (N + 1, N + 2))):
+            face = 2 * axis + side
+            for ghost in ghosts:
+                g = _face(cells, ndim, axis, ghost)
+                for c in range(ndim + 2):
+                    assert np.all(g[c] == inflow[face][c]), (axis, side, ghost, c)
+    interior = (slice(None),) + tuple(slice(2, d + 2) for d in dims[::-1])
+    assert np.array_equal(cells[interior], before[interior])
+    if ndim >= 2:
+        assert np.array_equal(cells[:, 0, 0], before[:, 0, 0])
+
+
 @pytest.mark.parametrize("ndim,dims", [(1, [32]), (2, [16, 8]), (3, [8, 8, 4])])
 def test_cfl_time_step(ndim, dims):
     """rhyme_cfl_dt_test.f90:58-73: dt = c*min(dx)/max(|v|+cs)."""
