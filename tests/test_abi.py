@@ -127,3 +127,29 @@ def test_header_is_plain_c_and_a_c_driver_links(lib, tmp_path, compiler, flags):
     out = subprocess.run([compiler, obj, "-L", build.OUT_DIR, "-lrhyme_gpu", "-o", exe],
                          capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
+
+
+def test_product_path_fails_loudly_without_a_gpu(lib):
+    """No CPU fallback: without a visible GPU, creating a context raises
+    RhymeGpuError(ECUDA) (parameter validation passes, the first CUDA call
+    fails); the server does the same."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    with pytest.raises(gpu.RhymeGpuError) as e:
+        gpu.Context(params.hydro_params(1))
+    assert e.value.code == gpu.ECUDA
+    with pytest.raises(gpu.RhymeGpuError) as e:
+        gpu.Server(params.hydro_params(3, precision=params.MIXED))
+    assert e.value.code == gpu.ECUDA
+
+
+def test_missing_library_raises_import_error(monkeypatch, tmp_path):
+    """Without the built library the binding raises at load, before any
+    call; nothing stands in for it."""
+    monkeypatch.setattr(gpu, "_lib", None)
+    monkeypatch.setattr(gpu, "LIB_PATH", str(tmp_path / "librhyme_gpu.so"))
+    with pytest.raises(ImportError):
+        gpu.load()
+    with pytest.raises(ImportError):
+        gpu.Context(params.hydro_params(1))
