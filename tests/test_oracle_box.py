@@ -96,6 +96,48 @@ def test_set_inflow_boundaries(ndim, dims):
         assert np.array_equal(cells[:, 0, 0], before[:, 0, 0])
 
 
+def _fill_1d_reference_order(c, n, bctype):
+    """The statements of rhyme_samr_bc_set_left_boundary.f90 then
+    _set_right_boundary.f90 (rhyme_samr_bc_set_boundaries.f90:9-10) for a
+    1-D box, on c[comp, i + 1] = cells(i, comp), i = -1 .. n + 2, in the
+    reference's order: left copies, left momentum sign, right copies, right
+    momentum sign."""
+    at = lambda i: i + 1  # noqa: E731
+    if bctype == 3:
+        c[:, at(0)] = c[:, at(n)]
+        c[:, at(-1)] = c[:, at(n - 1)]
+    else:
+        c[:, at(0)] = c[:, at(1)]
+        c[:, at(-1)] = c[:, at(2)]
+        if bctype == 1:
+            c[1, at(0)] = -c[1, at(1)]
+            c[1, at(-1)] = -c[1, at(2)]
+    if bctype == 3:
+        c[:, at(n + 1)] = c[:, at(1)]
+        c[:, at(n + 2)] = c[:, at(2)]
+    else:
+        c[:, at(n + 1)] = c[:, at(n)]
+        c[:, at(n + 2)] = c[:, at(n - 1)]
+        if bctype == 1:
+            c[1, at(n + 1)] = -c[1, at(n)]
+            c[1, at(n + 2)] = -c[1, at(n - 1)]
+    return c
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+@pytest.mark.parametrize("bctype", [1, 2, 3])
+def test_ghost_fill_order_on_short_boxes(n, bctype):
+    """With fewer than 4 interior cells a face's ghost layers read cells
+    that the other face writes (for n = 1 the left face's outer ghost reads
+    the right face's inner ghost before that face is filled), so the result
+    depends on the reference's statement order, which the oracle keeps."""
+    rng = np.random.default_rng(n * 10 + bctype)
+    cells = rng.uniform(0.5, 2.0, (3, n + 4))   # ghosts hold distinct old values
+    want = _fill_1d_reference_order(cells.copy(), n, bctype)
+    oracle.set_boundaries(_params(1, [bctype] * 6), cells)
+    assert np.array_equal(cells, want)
+
+
 @pytest.mark.parametrize("ndim,dims", [(1, [32]), (2, [16, 8]), (3, [8, 8, 4])])
 def test_cfl_time_step(ndim, dims):
     """rhyme_cfl_dt_test.f90:58-73: dt = c*min(dx)/max(|v|+cs)."""
