@@ -374,13 +374,14 @@ int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int
  *  - d_cells_in / d_cells_out: device pointers to the NDIM+2 hydro component
  *    blocks of the box in the layout of rhyme_gpu_register_box, ghosts of
  *    d_cells_in already filled. The interior of d_cells_out receives U^{n+1};
- *    its ghosts are not written. d_cells_out may equal d_cells_in.
+ *    its ghosts are not written. The two arrays must not overlap (an
+ *    in-place call is rejected with RHYME_GPU_EINVAL).
  *  - params->precision must be RHYME_GPU_FP64.
  *  - Scratch: a fixed device array of RHYME_GPU_NOALLOC_SCRATCH_DOUBLES
  *    doubles (16 MiB) inside this library, which every GPU that loads the
  *    library holds until the process exits. A box needs
- *    32 + 3*NDIM*(NDIM+2)*prod(N_a + 4) doubles (a 2-D 291^2 box, a 3-D
- *    32^3 box); larger boxes are rejected with RHYME_GPU_EINVAL and a
+ *    32 + 3*NDIM*(NDIM+2)*prod(N_a + 4) doubles (at most a 2-D 291^2 box
+ *    or a 3-D 31^3 box); larger boxes are rejected with RHYME_GPU_EINVAL and a
  *    message on stderr.
  *  - The first call on a device looks up the array's device address
  *    (cudaGetSymbolAddress) with that device current; make that first call

@@ -78,6 +78,14 @@ extern "C" int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params, const 
     return bad("box too large: needs %lld scratch doubles, the fixed scratch holds %lld", need,
                kScratchDoubles);
 
+  // The update reads U^n and writes U^{n+1} through restrict-qualified
+  // pointers, so the two state arrays must not share memory.
+  const long long bytes = (long long)(D + 2) * g.field * (long long)sizeof(double);
+  const char* in_lo = (const char*)d_cells_in;
+  const char* out_lo = (const char*)d_cells_out;
+  if (in_lo < out_lo + bytes && out_lo < in_lo + bytes)
+    return bad("d_cells_in and d_cells_out overlap; pass two separate state arrays");
+
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) return RHYME_GPU_ECUDA;
@@ -89,32 +97,7 @@ extern "C" int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params, const 
   }
 
   DevParams P;
-  memset(&P, 0, sizeof(P));
-  const double gm = params->gamma;
-  P.G.g = gm;
-  P.G.gm1 = gm - 1.0;
-  P.G.gp1 = gm + 1.0;
-  P.G.gm1_gp1 = P.G.gm1 / P.G.gp1;
-  P.G.gm1_2g = P.G.gm1 / (2.0 * gm);
-  P.G.gp1_2g = P.G.gp1 / (2.0 * gm);
-  P.G.g_inv = 1.0 / gm;
-  P.G.kb_amu = params->kb_amu;
-  P.G.two_gp1 = 2.0 / P.G.gp1;
-  P.G.two_gm1 = 2.0 / P.G.gm1;
-  P.G.inv_gm1_2g = 1.0 / P.G.gm1_2g;
-  P.G.gm1_half = 0.5 * P.G.gm1;
-  P.G.half_gm1 = P.G.gm1 / 2.0;
-  P.G.g_kb_amu = gm * params->kb_amu;
-  P.rp.vac_rho = params->vacuum_density;
-  P.rp.vac_p = params->vacuum_pressure;
-  P.rp.vac_rho_next = std::nextafter(params->vacuum_density, 1.0);
-  P.rp.tol = params->tolerance;
-  P.rp.n_iter = params->n_iteration;
-  P.ndim = D;
-  P.limiter = params->limiter;
-  P.omega = params->omega;
-  P.solver_type = params->solver_type;
-  P.courant = params->courant;
+  make_dev_params(params, &P);
 
   Dx d;
   for (int a = 0; a < 3; ++a) d.v[a] = (a < D) ? dx[a] : 1.0;

@@ -136,6 +136,13 @@ struct Dx {
   double min;  // minval(dx(1:NDIM))
 };
 
+}  // namespace rgpu
+struct rhyme_gpu_params;
+namespace rgpu {
+// The kernels' parameters from the C-ABI's (gas constants, Riemann and
+// limiter settings, boundary types), in rhyme_gpu.cu.
+void make_dev_params(const rhyme_gpu_params* p, DevParams* d);
+
 // Launchers (kernels_box.cu). All asynchronous on `st`.
 // *dst = v in stream order (a scalar from the host without a staging buffer).
 cudaError_t launch_set_double(double* dst, double v, cudaStream_t st);

@@ -181,7 +181,11 @@ int validate(rhyme_gpu_ctx* ctx, const rhyme_gpu_params* p) {
   return RHYME_GPU_OK;
 }
 
-void make_dev_params(const rhyme_gpu_params* p, DevParams* d) {
+}  // namespace
+
+// Declared in rgpu_internal.h: the allocation-free entry point builds its
+// kernel parameters with the same function.
+void rgpu::make_dev_params(const rhyme_gpu_params* p, DevParams* d) {
   memset(d, 0, sizeof(*d));
   const double g = p->gamma;
   Gas<double>& G = d->G;
@@ -214,6 +218,8 @@ void make_dev_params(const rhyme_gpu_params* p, DevParams* d) {
   }
   d->courant = p->courant;
 }
+
+namespace {
 
 void make_mixed_params(const DevParams& d, MixedParams* m) {
   memset(m, 0, sizeof(*m));

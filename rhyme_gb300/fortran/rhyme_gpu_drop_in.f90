@@ -98,6 +98,12 @@ contains
 
       integer(c_int) :: dims(3), h, rc
 
+      if (box%level < lbound(rhyme_gpu_handles, 1) .or. box%level > ubound(rhyme_gpu_handles, 1) &
+          .or. box%number < 1 .or. box%number > rhyme_gpu_max_boxes) then
+         call logger%err('box level or number outside the GPU handle table')
+         return
+      end if
+
       dims = 1
       dims(1:NDIM) = box%dims
       rc = rhyme_gpu_register_box(rhyme_gpu_ctx_ptr, box%level, box%number, box%cells, dims, &
@@ -116,6 +122,11 @@ contains
 
    pure integer(c_int) function rhyme_gpu_handle_of(box) result(h)
       type(samr_box_t), intent(in) :: box
+      ! a box outside the table was never registered: -1 makes every call
+      ! on it return RHYME_GPU_EINVAL
+      h = -1
+      if (box%level < lbound(rhyme_gpu_handles, 1) .or. box%level > ubound(rhyme_gpu_handles, 1)) return
+      if (box%number < 1 .or. box%number > rhyme_gpu_max_boxes) return
       h = rhyme_gpu_handles(box%level, box%number)
    end function rhyme_gpu_handle_of
 

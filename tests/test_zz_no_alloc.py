@@ -16,8 +16,6 @@ import oracle
 from rhyme_gb300 import gpu, ic
 from rhyme_gb300.params import hydro_params
 
-pytestmark = pytest.mark.gpu
-
 
 def _reference_step(p, cells, dx, dt):
     """One step through the existing entry point (rhyme_gpu_mh_solve)."""
@@ -55,6 +53,7 @@ def _interior(c, ndim):
     return c[(slice(None),) + (slice(2, -2),) * ndim]
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("ndim", [1, 2, 3])
 def test_noalloc_matches_existing_entry_point_twice(ndim):
     torch = pytest.importorskip("torch")
@@ -78,13 +77,43 @@ def test_noalloc_matches_existing_entry_point_twice(ndim):
         assert np.array_equal(_interior(got, ndim), _interior(ref, ndim))
 
 
-def test_noalloc_rejects_boxes_beyond_the_scratch():
-    lib = gpu.load()
-    p = hydro_params(3)
+def _call(lib, p, d_in, d_out, dims, dt=1e-3, stream=None):
     s = gpu.params_struct(p)
-    dims = np.array([64, 64, 64], dtype=np.int32)
+    dims = np.array(list(dims) + [1] * (3 - len(dims)), dtype=np.int32)
     dx3 = np.full(3, 1.0 / 64)
-    rc = lib.rhyme_gpu_mh_solve_noalloc(C.byref(s), C.c_void_p(16), C.c_void_p(16),
-                                        dims.ctypes.data_as(C.POINTER(C.c_int)),
-                                        dx3.ctypes.data_as(C.POINTER(C.c_double)), 1e-3, None)
-    assert rc == gpu.EINVAL
+    return lib.rhyme_gpu_mh_solve_noalloc(C.byref(s), C.c_void_p(d_in), C.c_void_p(d_out),
+                                          dims.ctypes.data_as(C.POINTER(C.c_int)),
+                                          dx3.ctypes.data_as(C.POINTER(C.c_double)), dt,
+                                          C.c_void_p(stream))
+
+
+# The scratch holds 2 Mi doubles and a box needs 32 + 3*D*(D+2)*prod(N+4):
+# 291^2 and 31^3 fit, 292^2 and 32^3 do not.
+@pytest.mark.parametrize("ndim,dims", [(2, (292, 292)), (3, (32, 32, 32)), (3, (64, 64, 64))])
+def test_noalloc_rejects_boxes_beyond_the_scratch(ndim, dims):
+    # rejected before any CUDA call, so the dummy pointers are never used
+    lib = gpu.load()
+    assert _call(lib, hydro_params(ndim), 1 << 20, 1 << 30, dims) == gpu.EINVAL
+
+
+def test_noalloc_rejects_overlapping_state_arrays():
+    lib = gpu.load()
+    p = hydro_params(1)
+    assert _call(lib, p, 1 << 20, 1 << 20, (64,)) == gpu.EINVAL
+    assert _call(lib, p, 1 << 20, (1 << 20) + 8, (64,)) == gpu.EINVAL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ndim,n", [(2, 291), (3, 31)])
+def test_noalloc_accepts_boxes_at_the_limit(ndim, n):
+    torch = pytest.importorskip("torch")
+    if ndim == 2:
+        cells, dx, p = ic.slab_2d(n=n, seed=6)
+    else:
+        cells, dx, p = ic.spheres_3d(n=n, nspheres=2, seed=6)
+    oracle.set_boundaries(p, cells)
+    dt = oracle.cfl_time_step(p, cells, dx)
+    stream = torch.cuda.current_stream().cuda_stream
+    got = _noalloc_step(p, cells, dx, dt, stream)
+    ref = _reference_step(p, cells, dx, dt)
+    assert np.array_equal(_interior(got, ndim), _interior(ref, ndim))
