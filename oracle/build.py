@@ -15,8 +15,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "oracle_capi.cpp")]
 DEPS = SOURCES + [os.path.join(HERE, "rhyme_oracle.hpp"),
-                  os.path.join(os.path.dirname(HERE), "rhyme_gb300", "csrc", "detmath.h"),
-                  os.path.join(os.path.dirname(HERE), "rhyme_gb300", "csrc", "detmath_tables.h")]
+                  os.path.join(os.path.dirname(HERE), "rhyme_gb300", "csrc", "libm_pow.h"),
+                  os.path.join(os.path.dirname(HERE), "rhyme_gb300", "csrc", "libm_pow_tables.h")]
 
 
 def needs_build():

@@ -46,17 +46,17 @@ static Params to_params(const oracle_params* p) {
 
 int oracle_abi_version(void) { return 1; }
 
-// 0: C library pow (as the compiled reference); 1: detmath::det_pow.
+// 0: C library pow (as the compiled reference); 1: libm_pow::pow (its restatement).
 int oracle_set_pow_mode(int mode) {
   if (mode != 0 && mode != 1) return -1;
   pow_mode() = mode;
   return 0;
 }
 
-// det_pow and the C library pow over n (x, y) pairs, for the ulp check.
-int oracle_pow_pair(const double* x, const double* y, long long n, double* det, double* lib) {
+// libm_pow::pow and the C library pow over n (x, y) pairs, for the bit check.
+int oracle_pow_pair(const double* x, const double* y, long long n, double* mine, double* lib) {
   for (long long i = 0; i < n; ++i) {
-    det[i] = detmath::det_pow(x[i], y[i]);
+    mine[i] = libm_pow::pow(x[i], y[i]);
     lib[i] = std::pow(x[i], y[i]);
   }
   return 0;

@@ -83,8 +83,8 @@ def lib():
 
 
 def set_pow_mode(mode):
-    """0: C library pow (as the compiled reference); 1: det_pow (bit-exact
-    with the CUDA library). Returns the previous mode."""
+    """0: C library pow (as the compiled reference); 1: libm_pow::pow, its
+    restatement that the CUDA library runs. Returns the previous mode."""
     global _pow_mode
     prev = _pow_mode
     if lib().oracle_set_pow_mode(int(mode)) != 0:
@@ -110,11 +110,12 @@ class pow_mode:
 
 
 def pow_pair(x, y):
+    """(restated pow, C library pow) of the same arguments."""
     x, y = _f64(x), _f64(y)
-    det = np.zeros_like(x)
+    mine = np.zeros_like(x)
     libv = np.zeros_like(x)
-    lib().oracle_pow_pair(_d(x), _d(y), x.size, _d(det), _d(libv))
-    return det, libv
+    lib().oracle_pow_pair(_d(x), _d(y), x.size, _d(mine), _d(libv))
+    return mine, libv
 
 
 def _d(a):

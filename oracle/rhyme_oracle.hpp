@@ -29,21 +29,21 @@
 #include <cstring>
 #include <vector>
 
-#include "../rhyme_gb300/csrc/detmath.h"
+#include "../rhyme_gb300/csrc/libm_pow.h"
 
 namespace rhyme_oracle {
 
 // Power function used for every real `**` of the reference. Mode 0 is the C
-// library's pow, as the compiled Fortran calls it; mode 1 is
-// detmath::det_pow, the deterministic power function the CUDA library uses
-// (within one ulp of the C library's, see tests/test_oracle_golden.py), so
-// the GPU can be checked bit for bit.
+// library's pow, as the compiled Fortran calls it: the reference arithmetic
+// the GPU is checked against. Mode 1 is libm_pow::pow, the restatement of
+// that function which the CUDA library runs; it lets the tests show, on the
+// CPU, that the restatement returns the C library's bits.
 inline int& pow_mode() {
   static int mode = 0;
   return mode;
 }
 inline double opow(double x, double y) {
-  return pow_mode() == 1 ? detmath::det_pow(x, y) : std::pow(x, y);
+  return pow_mode() == 1 ? libm_pow::pow(x, y) : std::pow(x, y);
 }
 
 // tiny(0d0) in Fortran is the smallest positive normal double.

@@ -43,7 +43,7 @@ UNITS = [
     ("kernels_sanity", "kernels_sanity.cu", ["--fmad=false"]),
     ("kernels_paint", "kernels_paint.cu", ["--fmad=false"]),
 ]
-HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "detmath_tables.h", "box_elems.cuh", "sweep.cuh"]
+HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "libm_pow.h", "libm_pow_tables.h", "box_elems.cuh", "sweep.cuh"]
 
 
 def nvcc():

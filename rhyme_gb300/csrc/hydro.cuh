@@ -18,17 +18,18 @@
 #include <cfloat>
 #include <cstdint>
 
-#include "detmath.h"
+#include "libm_pow.h"
 
 namespace rgpu {
 
 // ---- math by type --------------------------------------------------------
-// Double powers go through detmath::det_pow, which the CPU oracle can run
-// bit for bit, so the FP64 path and its checker agree exactly even in flows
-// that amplify a one-ulp difference.
+// Double powers go through libm_pow::pow, a restatement of the C library's
+// pow that the compiled reference calls for every real `**`, so the FP64 path
+// returns the reference's bits even in flows that amplify a one-ulp
+// difference.
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
-__device__ __forceinline__ double m_pow(double x, double y) { return detmath::det_pow(x, y); }
+__device__ __forceinline__ double m_pow(double x, double y) { return libm_pow::pow(x, y); }
 // Float powers as 2^(y log2 x) with CUDA's log2f and exp2f: the rounding of
 // the product adds a relative error of about 2^-24 |y log2 x| to the result
 // (for the positive bases of this path), against powf's ~1 ulp, for a
@@ -36,7 +37,7 @@ __device__ __forceinline__ double m_pow(double x, double y) { return detmath::de
 __device__ __forceinline__ float m_pow(float x, float y) { return exp2f(y * log2f(x)); }
 // x**y1 and x**y2 of one base (one logarithm).
 __device__ __forceinline__ void m_pow2(double x, double y1, double y2, double& r1, double& r2) {
-  detmath::det_pow2(x, y1, y2, &r1, &r2);
+  libm_pow::pow2(x, y1, y2, &r1, &r2);
 }
 __device__ __forceinline__ void m_pow2(float x, float y1, float y2, float& r1, float& r2) {
   const float l = log2f(x);

@@ -31,8 +31,7 @@ def test_spheres_256_fp64_bitwise(spheres256):
         dts = ctx.run(b, dx, 3)
         ctx.sync_to_host(b)
     ref = cells.copy()
-    with oracle.pow_mode(1):
-        dref = oracle.run(p, ref, dx, 3, nthreads=NTHREADS)
+    dref = oracle.run(p, ref, dx, 3, nthreads=NTHREADS)
     assert np.array_equal(dts, dref)
     assert np.array_equal(got, ref)
 
@@ -75,7 +74,6 @@ def test_batch4096_boxes_fp64_bitwise():
             ctx.sync_to_host(h)
     for i, (st, (cells, dx, p)) in enumerate(zip(states, boxes)):
         ref = cells.copy()
-        with oracle.pow_mode(1):
-            dref = oracle.run(p, ref, dx, 10, nthreads=NTHREADS)
+        dref = oracle.run(p, ref, dx, 10, nthreads=NTHREADS)
         assert dts[i] == dref[-1], pick[i]
         assert np.array_equal(st, ref, equal_nan=True), pick[i]

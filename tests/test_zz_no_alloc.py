@@ -73,7 +73,7 @@ def test_noalloc_matches_existing_entry_point_twice(ndim):
         ref = _reference_step(p, state, dx, dt)
         got = _noalloc_step(p, state, dx, dt, stream)
         # same kernels, same arithmetic: identical interiors (the FP64 tests'
-        # tolerance is bit-identity with the det-pow oracle)
+        # tolerance is bit-identity with the oracle)
         assert np.array_equal(_interior(got, ndim), _interior(ref, ndim))
 
 
