@@ -5,7 +5,10 @@ density ripple (superbee, courant 0.3, gamma 5/3), in the mixed FP32/FP64
 form, with the plain FP64 path timed on the same box beside it and the
 per-field L1 / Linf difference between the two after 300 steps: the
 configuration the mixed-vs-FP64 metric is quoted on. A step is one driver
-iteration (dt -> ghost fill -> solve) over the box.
+iteration (dt -> ghost fill -> solve) over the box. Every arm first advances
+the box untimed to the middle of its run (--advance, default half the
+workload's step count: step 150 of the 300-step sphere run), so the timed
+window sees the developed flow rather than the nearly uniform start.
 
   value   cell-updates/s with the state resident in HBM, timed with CUDA
           events on the library's stream around each step; L2 is flushed
@@ -29,8 +32,9 @@ Other workloads (--workload): slab2d (2-D 256^2 shear slab, plain FP64,
 seeded Poisson stream of requests served by the continuous-batching server
 against one-at-a-time plain FP64).
 
---impl reference times the CPU implementation alone on the same config
-(with --cpu-threads N, on N OpenMP threads).
+--impl reference times the CPU implementation alone on the same config and
+window: the whole box, advanced by the CPU itself (with --cpu-threads N, on
+N OpenMP threads).
 Under torchrun each rank runs an independent replica (the path shards by
 box; a single box is replicated) and value is the sum over ranks.
 """
@@ -181,7 +185,9 @@ def ncu_traffic(workload_name, kernel):
 
 
 def cpu_sample(cells, dx, p, steps_cap, budget_s, nthreads):
-    """Oracle cell-updates/s on the first steps of the workload (bounded)."""
+    """Oracle cell-updates/s stepping `cells` (bounded by steps_cap steps and
+    about budget_s seconds; the first step, which allocates the workspace,
+    is untimed)."""
     import oracle
     c = cells.copy()
     interior = int(np.prod([s - 4 for s in c.shape[1:]]))
@@ -238,17 +244,14 @@ def launches_per_step(prec, ndim):
     return 5 if prec == "fp64" else 3 + ndim
 
 
-def reference_sample(name, cells, dx, p, cfg):
-    """The bounded sample one reference-arm step runs: the whole box, or for
-    3-D boxes of 128^3 and more its first 16 z-planes (with the box's own
-    periodic boundaries), so that a step takes well under a second."""
-    if cfg["ndim"] == 3 and cells.shape[1] - 4 >= 128:
-        nz = 16
-        sub = np.ascontiguousarray(cells[:, :nz + 4])
-        n = int(np.prod([s - 4 for s in sub.shape[1:]]))
-        return sub, n, "first %d z-planes of the %s box (%d cells) per step" % (
-            nz, "x".join(str(s - 4) for s in cells.shape[1:][::-1]), n)
-    return cells.copy(), cfg["cells"], "the whole box per step"
+def advance_steps(args, cfg):
+    """Untimed steps before the warm-up: half the workload's run by default."""
+    return cfg["steps_in_run"] // 2 if args.advance is None else args.advance
+
+
+def window_text(adv, W, K, cfg):
+    return "steps %d-%d of the %d-step run (advanced %d steps untimed, then %d warm-up steps)" % (
+        adv + W + 1, adv + W + K, cfg["steps_in_run"], adv, W)
 
 
 REF_BATCH_BOXES = 64
@@ -309,15 +312,19 @@ def run_reference(args, rank, world):
     p = dict(p, precision=FP64)  # the CPU implementation is FP64
     import oracle
     nthreads = args.cpu_threads or os.cpu_count() or 1
-    c, n, what = reference_sample(args.workload, cells, dx, p, cfg)
+    c, n = cells.copy(), cfg["cells"]
+    adv = advance_steps(args, cfg)
+    if adv:
+        oracle.run(p, c, dx, adv, nthreads=nthreads)
     if args.warmup:
         oracle.run(p, c, dx, args.warmup, nthreads=nthreads)
     t0 = time.perf_counter()
     oracle.run(p, c, dx, args.steps, nthreads=nthreads)
     t = time.perf_counter() - t0
     v = n * args.steps / t
-    sample = "%d timed steps after %d warm-up steps; %s; OpenMP over the outer cell loop" % (
-        args.steps, args.warmup, what)
+    sample = "the whole box (%d cells), %s; OpenMP over the outer cell loop" % (
+        n, window_text(adv, args.warmup, args.steps, cfg))
+    cfg = dict(cfg, window=window_text(adv, args.warmup, args.steps, cfg))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -365,11 +372,17 @@ def run_gpu(args, rank, local, world):
     clocks.start()
     time.sleep(0.3)
 
-    # headline form
+    adv = advance_steps(args, cfg)
+
+    # headline form, advanced untimed to the window
     ctx = gpu.Context(p)
     state = cells.copy()
     box = ctx.register_box(state)
     stream = torch.cuda.ExternalStream(ctx.stream)
+    if adv:
+        ctx.run(box, dx, adv, trace=False)
+        ctx.sync_to_host(box)
+        np.copyto(host, state)  # the end-to-end loop starts from the same state
     ctx.run(box, dx, W, trace=False)
     ctx.synchronize()
     barrier(world)
@@ -384,12 +397,19 @@ def run_gpu(args, rank, local, world):
 
     # plain FP64 on the same box, and the difference after the run's steps
     cmp = None
+    cpu_state = cells  # the CPU baseline's starting state (the window's)
     if compare:
         pc = dict(p, precision=FP64)
         ctx_c = gpu.Context(pc)
         state_c = cells.copy()
         box_c = ctx_c.register_box(state_c)
         stream_c = torch.cuda.ExternalStream(ctx_c.stream)
+        if adv:
+            ctx_c.run(box_c, dx, adv, trace=False)
+            ctx_c.sync_to_host(box_c)
+            # the FP64 path is bit-identical to the CPU oracle, so this is
+            # the oracle's own state at the window
+            cpu_state = state_c.copy()
         ctx_c.run(box_c, dx, W, trace=False)
         ctx_c.synchronize()
         barrier(world)
@@ -399,10 +419,10 @@ def run_gpu(args, rank, local, world):
         tc1 = time.time()
         ms_c = allmax(sum(per_c), world)
         value_c = world * interior * K / (ms_c * 1e-3)
-        n_acc = max(cfg["steps_in_run"], W + K)
+        n_acc = max(cfg["steps_in_run"], adv + W + K)
         for c_, b_ in ((ctx, box), (ctx_c, box_c)):
-            if n_acc > W + K:
-                c_.run(b_, dx, n_acc - (W + K), trace=False)
+            if n_acc > adv + W + K:
+                c_.run(b_, dx, n_acc - (adv + W + K), trace=False)
             c_.sync_to_host(b_)
         fb = ctx.fallback_count(box)
         errs = field_errors(state, state_c, ndim)
@@ -462,9 +482,16 @@ def run_gpu(args, rank, local, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = args.cpu_threads or os.cpu_count() or 1
-        v, n, t = cpu_sample(cells, dx, dict(p, precision=FP64), cfg["steps_in_run"], args.cpu_budget, nthreads)
+        if adv and cpu_state is cells:
+            # no FP64 run on the GPU: the oracle advances the box itself
+            cpu_state = cells.copy()
+            import oracle
+            oracle.run(dict(p, precision=FP64), cpu_state, dx, adv, nthreads=nthreads)
+        v, n, t = cpu_sample(cpu_state, dx, dict(p, precision=FP64), cfg["steps_in_run"] - adv,
+                             args.cpu_budget, nthreads)
         cpu = {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
-               "sample": "first %d steps of the same workload (%.1f s), CPU oracle (FP64), OpenMP" % (n, t)}
+               "sample": "the whole box, %d steps from step %d of the same workload (%.1f s), CPU oracle "
+                         "(FP64), OpenMP" % (n, adv, t)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
@@ -472,7 +499,8 @@ def run_gpu(args, rank, local, world):
                 "ms_per_step_max": max(per_step), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": dtype_name(prec), "data": "synthetic",
                 "config": dict(cfg, l2="flushed (512 MiB write) between timed steps, outside the events",
-                               parallelism="replicas" if world > 1 else "single box"),
+                               parallelism="replicas" if world > 1 else "single box",
+                               window=window_text(adv, W, K, cfg)),
                 "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": hydro_bytes + 8,
                         "d2h_bytes_per_step": hydro_bytes + 8 + 4, "steps": ke,
                         "windows": windows, "statistic": "median of %d windows of %d steps" % (E2E_WINDOWS, ke)},
@@ -645,6 +673,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the other precision")
+    ap.add_argument("--advance", type=int, default=None,
+                    help="untimed steps before the warm-up (default: half the workload's run)")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -157,7 +157,8 @@ def test_full_component_layout_resident_run(ndim, precision):
     with gpu.Context(dict(p, precision=precision)) as ctx:
         b = ctx.register_box(full)
         dts = ctx.run(b, dx, steps)
-        ctx.sync_to_device(b)  # a second upload from the host array
+        ctx.sync_to_host(b)
+        ctx.sync_to_device(b)  # a second upload, from the downloaded host array
         dts2 = ctx.run(b, dx, 2)
         ctx.sync_to_host(b)
     assert np.array_equal(full[ndim + 2:], sentinels)
@@ -171,6 +172,7 @@ def test_full_component_layout_resident_run(ndim, precision):
         with gpu.Context(dict(p, precision=MIXED)) as ctx:
             b = ctx.register_box(alone)
             ctx.run(b, dx, steps)
+            ctx.sync_to_host(b)
             ctx.sync_to_device(b)
             ctx.run(b, dx, 2)
             ctx.sync_to_host(b)
