@@ -55,6 +55,9 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-updates/s"
 L2_FLUSH_BYTES = 512 << 20
 DEFAULT_WORKLOAD = "spheres3d256"
+SERVE_REQUESTS = 512      # p99 over a stream of this many requests
+SERVE_FP64_PREFIX = 48    # the one-at-a-time FP64 baseline serves this prefix
+SERVE_ERR_REQUESTS = 24   # served results replayed alone in FP64 for the error
 E2E_WINDOWS = 5
 
 
@@ -404,13 +407,11 @@ def run_gpu(args, rank, local, world):
         state_c = cells.copy()
         box_c = ctx_c.register_box(state_c)
         stream_c = torch.cuda.ExternalStream(ctx_c.stream)
-        if adv:
-            ctx_c.run(box_c, dx, adv, trace=False)
-            ctx_c.sync_to_host(box_c)
-            # the FP64 path is bit-identical to the CPU oracle, so this is
-            # the oracle's own state at the window
-            cpu_state = state_c.copy()
-        ctx_c.run(box_c, dx, W, trace=False)
+        ctx_c.run(box_c, dx, adv + W, trace=False)
+        ctx_c.sync_to_host(box_c)
+        # the FP64 path is bit-identical to the CPU oracle, so this is the
+        # oracle's own state at the timed window
+        cpu_state = state_c.copy()
         ctx_c.synchronize()
         barrier(world)
         tc0 = time.time()
@@ -482,16 +483,17 @@ def run_gpu(args, rank, local, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthreads = args.cpu_threads or os.cpu_count() or 1
-        if adv and cpu_state is cells:
+        start = adv + W
+        if cpu_state is cells:
             # no FP64 run on the GPU: the oracle advances the box itself
             cpu_state = cells.copy()
             import oracle
-            oracle.run(dict(p, precision=FP64), cpu_state, dx, adv, nthreads=nthreads)
-        v, n, t = cpu_sample(cpu_state, dx, dict(p, precision=FP64), cfg["steps_in_run"] - adv,
+            oracle.run(dict(p, precision=FP64), cpu_state, dx, start, nthreads=nthreads)
+        v, n, t = cpu_sample(cpu_state, dx, dict(p, precision=FP64), max(1, cfg["steps_in_run"] - start),
                              args.cpu_budget, nthreads)
         cpu = {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port",
-               "sample": "the whole box, %d steps from step %d of the same workload (%.1f s), CPU oracle "
-                         "(FP64), OpenMP" % (n, adv, t)}
+               "sample": "the whole box, %d timed steps after step %d of the same workload (%.1f s), CPU "
+                         "oracle (FP64), OpenMP" % (n, start + 1, t)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
@@ -579,10 +581,17 @@ def run_batch(args, rank, local, world):
         dm = np.zeros(5)
         sm = np.zeros(5)
         bad64, bad_mixed_only, used = 0, 0, 0
+        def physical(c):
+            # finite, positive density and positive pressure (gamma 5/3)
+            if not np.isfinite(c).all() or c[0].min() <= 0:
+                return False
+            ke = 0.5 * (c[1] ** 2 + c[2] ** 2 + c[3] ** 2) / c[0]
+            return bool(((c[4] - ke) * (2.0 / 3.0)).min() > 0)
+
         for x, y in zip(a, b):
             xi, yi = x[:, 2:-2, 2:-2, 2:-2], y[:, 2:-2, 2:-2, 2:-2]
-            ok64 = bool(np.isfinite(yi).all() and yi[0].min() > 0)
-            okm = bool(np.isfinite(xi).all() and xi[0].min() > 0)
+            ok64 = physical(yi)
+            okm = physical(xi)
             if not ok64:
                 bad64 += 1
                 continue
@@ -598,8 +607,8 @@ def run_batch(args, rank, local, world):
             sm = np.maximum(sm, r.max(1))
         names = ["rho", "rho_vx", "rho_vy", "rho_vz", "e_tot"]
         cmp = {"after_steps": W + K, "definition": "relative L1 = sum|d|/sum|f64|, relative Linf = "
-               "max|d|/max|f64| over the interiors of the boxes that stay finite with positive density "
-               "in FP64", "boxes_compared": used,
+               "max|d|/max|f64| over the interiors of the boxes whose FP64 state after the run is "
+               "physical (finite, positive density and pressure)", "boxes_compared": used,
                "boxes_failing_in_fp64": bad64, "boxes_failing_in_mixed_only": bad_mixed_only,
                "l1": dict(zip(names, (d1 / s1).tolist())), "linf": dict(zip(names, (dm / sm).tolist()))}
     if rank == 0:
@@ -629,17 +638,45 @@ def run_serve(args, rank, local, world):
     from rhyme_gb300 import serving
     from rhyme_gb300.params import FP64, MIXED, hydro_params
     torch.cuda.set_device(local)
-    stream = serving.make_stream(n=args.requests, rate=args.rate, seed=rank)
+    nreq = args.requests if args.requests is not None else SERVE_REQUESTS
+    stream = serving.make_stream(n=nreq, rate=args.rate, seed=rank)
     out = {}
-    for name, prec, cap, paint in (("continuous_mixed", MIXED, 256, False),
-                                   ("continuous_mixed_painted", MIXED, 256, True),
-                                   ("one_at_a_time_fp64", FP64, 1, False)):
-        r = serving.replay(stream, hydro_params(3, precision=prec), hbm_budget=150 << 30, max_active=cap,
+    served = None
+    for name, prec, cap, paint, reqs in (("continuous_mixed", MIXED, 256, False, stream),
+                                         ("continuous_mixed_painted", MIXED, 256, True, stream),
+                                         ("one_at_a_time_fp64", FP64, 1, False, stream[:SERVE_FP64_PREFIX])):
+        r = serving.replay(reqs, hydro_params(3, precision=prec), hbm_budget=150 << 30, max_active=cap,
                            paint=paint)
         lat = r["latencies"]
         out[name] = {"value": r["cell_updates"] / r["makespan"], "p50_s": float(np.percentile(lat, 50)),
                      "p99_s": float(np.percentile(lat, 99)), "makespan_s": r["makespan"],
-                     "cell_updates": r["cell_updates"], "peak_active": r["peak_active"]}
+                     "cell_updates": r["cell_updates"], "peak_active": r["peak_active"], "requests": len(reqs)}
+        if name == "continuous_mixed":
+            served = r["results"]
+    out["one_at_a_time_fp64"]["note"] = ("the first %d requests of the stream, at their arrival times"
+                                         % min(SERVE_FP64_PREFIX, nreq))
+    # per-request error of the served (mixed) results against each request
+    # replayed alone in FP64, over a seeded subset
+    from rhyme_gb300.metrics import field_errors
+    pick = sorted(np.random.default_rng(1).choice(nreq, size=min(SERVE_ERR_REQUESTS, nreq), replace=False))
+    per = []
+    names = ["rho", "rho_v1", "rho_v2", "rho_v3", "e_tot"]
+    for i in pick:
+        q = stream[i]
+        ref = serving.run_alone(q, hydro_params(3), FP64)
+        e = field_errors(served[i], ref, q["ndim"])
+        fields = [names[0]] + names[1:1 + q["ndim"]] + [names[4]]
+        per.append({"request": int(i), "ndim": q["ndim"], "dims": q["dims"], "steps": q["nsteps"],
+                    "l1": dict(zip(fields, [x[0] for x in e])), "linf": dict(zip(fields, [x[1] for x in e]))})
+    finite = [x for x in per if all(np.isfinite(v) for v in x["l1"].values())]
+    errs = {"requests": len(per), "definition": "per request and field: relative L1 = sum|d|/sum|f64|, "
+            "relative Linf = max|d|/max|f64| over the interior; the served mixed result against the "
+            "request replayed alone in plain FP64",
+            "max_l1": {f: max((x["l1"].get(f, 0.0) for x in finite), default=None) for f in names},
+            "max_linf": {f: max((x["linf"].get(f, 0.0) for x in finite), default=None) for f in names},
+            "median_l1_rho": float(np.median([x["l1"]["rho"] for x in finite])) if finite else None,
+            "requests_over_1e-6_l1_rho": sum(1 for x in finite if x["l1"]["rho"] > 1e-6),
+            "per_request": per}
     # capacity: the same requests all submitted at once (painted on the device)
     burst = [dict(q, arrival=0.0) for q in stream]
     r = serving.replay(burst, hydro_params(3, precision=MIXED), hbm_budget=150 << 30, max_active=256, paint=True)
@@ -651,13 +688,14 @@ def run_serve(args, rank, local, world):
     value = allsum(h["value"], world)
     if rank == 0:
         cu = sum(int(np.prod([s - 4 for s in q["cells"].shape[1:]])) * q["nsteps"] for q in stream)
-        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.requests,
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": nreq,
                 "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": {"workload": "Poisson stream, %d requests at %.3g/s, seed 0; 1-/2-/3-D equiprobable, "
                                        "cells log-uniform in [256, 128^3], 50-500 steps; 150 GB budget"
-                                       % (args.requests, args.rate), "cell_updates": cu},
-                "latency_s": {"p50": h["p50_s"], "p99": h["p99_s"]},
+                                       % (nreq, args.rate), "cell_updates": cu},
+                "latency_s": {"p50": h["p50_s"], "p99": h["p99_s"], "requests": nreq},
+                "errors_vs_fp64": errs,
                 "e2e": {"value": value, "unit": METRIC, "note": "host arrays in, results drained to host"},
                 "forms": out,
                 "throughput_over_one_at_a_time": h["value"] / out["one_at_a_time_fp64"]["value"]}
@@ -681,7 +719,8 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0,
                     help="OpenMP threads of the CPU oracle legs (default: every core)")
     ap.add_argument("--nboxes", type=int, default=4096)
-    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--requests", type=int, default=None,
+                    help="requests of the serve workload (default %d)" % SERVE_REQUESTS)
     ap.add_argument("--rate", type=float, default=8.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.workload != "serve":

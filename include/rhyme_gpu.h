@@ -363,6 +363,15 @@ int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int
                          int tile_pencils[3]);
 
 /*
+ * Instrumentation (no reference counterpart): how many single-box sweep
+ * launches of this process staged their slabs with TMA tensor copies
+ * (2-/3-D boxes whose x extent plus ghosts is a multiple of 4 cells; the
+ * others, and every launch with RHYME_GPU_TMA=0 in the environment, stage
+ * with coalesced loads and give the same results).
+ */
+int rhyme_gpu_tma_launches(long long* n);
+
+/*
  * No counterpart in the reference: one plain-FP64 MUSCL-Hancock update
  * (the same kernels as rhyme_gpu_mh_solve) that allocates nothing, for
  * callers that cannot allocate device memory: hosts whose device arrays come
@@ -463,6 +472,12 @@ int rhyme_gpu_server_create(const rhyme_gpu_params* base, const double courant[3
                             long long hbm_budget_bytes, int max_active,
                             rhyme_gpu_server** server);
 int rhyme_gpu_server_submit(rhyme_gpu_server* server, const rhyme_gpu_request* req, int* id);
+/* One tick: finished downloads land in the callers' arrays, pending requests
+ * are admitted in arrival order against the budget and the active cap, then
+ * every active request advances by the same number of steps (as many as the
+ * request nearest to completion still needs, 1 to 8; a batch whose
+ * membership has not changed since its last tick replays CUDA graphs), and
+ * finished requests start their download. */
 int rhyme_gpu_server_tick(rhyme_gpu_server* server, int* n_active, int* n_pending,
                           int* n_draining);
 /* state (RHYME_GPU_REQ_*), times = (submitted, admitted, done) in seconds

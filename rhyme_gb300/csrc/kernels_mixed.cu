@@ -35,6 +35,11 @@
 // so that finished rows can be copied back while the next slab is solved.
 #include <math_constants.h>
 
+#include <atomic>
+#include <cstdint>
+#include <cstdlib>
+
+#include "../../include/rhyme_gpu.h"
 #include "rgpu_internal.h"
 
 namespace rgpu {
@@ -542,5 +547,73 @@ cudaError_t launch_batch_sweeps(const MixedParams& M, const BoxDesc* TB, const B
   }
   return e;
 }
+
+// ---- tensor maps of the FP32 mirror (TMA staging of the sweeps) --------------
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+std::atomic<long long> g_tma_launches{0};
+
+EncodeTiledFn encoder() {
+  const char* env = getenv("RHYME_GPU_TMA");
+  if (env && env[0] == '0') return nullptr;
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return (EncodeTiledFn)p;
+  }();
+  return fn;
+}
+
+}  // namespace
+
+bool encode_mirror_map(CUtensorMap* out, const float* Uf, const Geom& g, int D, int A, int S, int P) {
+  if (D < 2 || A < 0 || A >= D) return false;
+  const EncodeTiledFn fn = encoder();
+  if (!fn) return false;
+  const long long X = g.s[1], Y = g.s[2] / g.s[1], Z = g.field / g.s[2];
+  // rows (and so every stride) a multiple of 16 bytes; base 16-byte aligned
+  if (X % 4 != 0 || ((uintptr_t)Uf % 16) != 0) return false;
+  cuuint64_t dim[4] = {(cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(D + 2)};
+  cuuint64_t stride[3] = {(cuuint64_t)X * 4, (cuuint64_t)(X * Y) * 4, (cuuint64_t)g.field * 4};
+  // the slab: S+4 cells along A; along x P pencils (A = y, z: P+4 cells from
+  // an aligned start); one cell along the third axis
+  cuuint32_t box[4] = {1, 1, 1, (cuuint32_t)(D + 2)};
+  box[A] = (cuuint32_t)(S + 4);
+  if (A == 0) {
+    box[1] = (cuuint32_t)P;
+  } else {
+    box[0] = (cuuint32_t)(P + 4);
+  }
+  for (int i = 0; i < 4; ++i)
+    if (box[i] > 256 || box[i] > dim[i]) return false;
+  if ((box[0] * 4) % 16 != 0) return false;
+  cuuint32_t estride[4] = {1, 1, 1, 1};
+  const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)Uf, dim, stride, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  g_tma_launches.fetch_add(1, std::memory_order_relaxed);
+  return true;
+}
+
+}  // namespace rgpu
+
+extern "C" int rhyme_gpu_tma_launches(long long* n) {
+  if (!n) return RHYME_GPU_EINVAL;
+  *n = rgpu::g_tma_launches.load(std::memory_order_relaxed);
+  return RHYME_GPU_OK;
+}
+
+namespace rgpu {
 
 }  // namespace rgpu

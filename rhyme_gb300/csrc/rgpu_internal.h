@@ -1,6 +1,7 @@
 // rgpu_internal.h -- types shared by the kernels and the C-ABI layer.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "hydro.cuh"
@@ -158,6 +159,15 @@ cudaError_t launch_mh_solve(const DevParams& P, const double* U, double* Unew, c
                             const Dx& dx, const StepScratch& s, cudaStream_t st,
                             cudaEvent_t* ev = nullptr);
 int max_cfl_blocks();
+
+// A 4-D tensor map (x, y, z, component) of a box's FP32 mirror Uf whose
+// copy box is the staged slab of a sweep along axis A with tiles of S cells
+// by P pencils (kernels_mixed.cu). False where a tensor copy cannot be used:
+// 1-D boxes, rows of the mirror not a multiple of 16 bytes, a slab larger
+// than the array, the driver's encoder unavailable, or RHYME_GPU_TMA=0 in
+// the environment. The sweeps then stage with coalesced loads (same
+// results).
+bool encode_mirror_map(CUtensorMap* out, const float* Uf, const Geom& g, int D, int A, int S, int P);
 
 // Mixed-precision launchers (kernels_mixed.cu).
 cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st);

@@ -1443,6 +1443,7 @@ struct rhyme_gpu_batch {
   FallbackQueue q{};
   int* qblock = nullptr;  // n, status, total
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int runs = 0;  // batch_run calls since the tables were built
 };
 
 namespace {
@@ -1474,6 +1475,7 @@ int batch_build(rhyme_gpu_batch* B) {
   batch_free(B);
   B->base_cur.resize(n);
   B->k = 0;
+  B->runs = 0;
   // order: largest boxes first (the queues hand them out first)
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
@@ -1664,10 +1666,13 @@ extern "C" int rhyme_gpu_batch_run(rhyme_gpu_batch* B, int nsteps) {
       break;
     }
   }
-  if (nsteps >= 4 && !B->graph[0]) {
+  // a CUDA graph per parity once the batch runs several steps, in one call
+  // or over repeated calls (a server stepping a stable set of requests)
+  if ((nsteps >= 4 || B->runs >= 2) && nsteps > 0 && !B->graph[0]) {
     int rc = batch_capture(B);
     if (rc != RHYME_GPU_OK) return rc;
   }
+  B->runs++;
   for (int s = 0; s < nsteps; ++s) {
     if (B->graph[0])
       CK(cudaGraphLaunch(B->graph[B->k], ctx->stream));
@@ -1908,7 +1913,15 @@ int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, in
     S->dirty[k] = true;
     S->pend_head++;
   }
-  // 3. one step of every active request, one batch per dimensionality
+  // 3. steps of every active request, one batch per dimensionality: as many
+  // as the request nearest to completion still needs (its retirement frees
+  // budget for the pending ones), at most kMaxTickSteps, so that arrivals
+  // wait at most that many steps to be admitted
+  constexpr int kMaxTickSteps = 8;
+  int tick_steps = kMaxTickSteps;
+  for (int k = 0; k < 3; ++k)
+    for (int id : S->active[k]) tick_steps = std::min(tick_steps, S->reqs[id].r.nsteps - S->reqs[id].steps_done);
+  tick_steps = std::max(tick_steps, 1);
   for (int k = 0; k < 3; ++k) {
     if (S->active[k].empty()) continue;
     rhyme_gpu_ctx* ctx = S->ctx[k];
@@ -1924,11 +1937,11 @@ int rhyme_gpu_server_tick(rhyme_gpu_server* S, int* n_active, int* n_pending, in
       if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
       S->dirty[k] = false;
     }
-    int rc = rhyme_gpu_batch_run(S->batch[k], 1);
+    int rc = rhyme_gpu_batch_run(S->batch[k], tick_steps);
     if (rc != RHYME_GPU_OK) return server_fail(S, rc, ctx->err.c_str());
     for (int id : S->active[k]) {
-      S->reqs[id].steps_done++;
-      S->cell_updates += S->reqs[id].cells;
+      S->reqs[id].steps_done += tick_steps;
+      S->cell_updates += S->reqs[id].cells * tick_steps;
     }
   }
   // 4. retire finished requests: download on the copy stream, free in order

@@ -2,7 +2,9 @@
 //
 // A CTA of TileCfg<S,P>::threads threads stages a slab of the FP32 mirror Uf (S
 // cells along the sweep axis plus the 2-cell ghost/halo layer, for P
-// pencils) in shared memory with coalesced loads, computes FP32 limited
+// pencils) in shared memory -- with one TMA tensor copy (cp.async.bulk.tensor
+// over a 4-D map of the mirror, completion on an mbarrier) where the mirror's
+// rows are 16-byte aligned, else with coalesced loads -- computes FP32 limited
 // slopes and half-step face states for S+2 cells, solves the S+1 exact
 // Riemann problems of the slab in FP32 (one thread per interface) and forms
 // the flux difference of its S cells. The tile shape (S, P) is a template
@@ -10,10 +12,62 @@
 // the autotuner, once per dimensionality.
 #pragma once
 
+#include <cuda.h>
+
 #include "rgpu_internal.h"
 
 namespace rgpu {
 namespace {
+
+// ---- TMA staging ------------------------------------------------------------
+// Bounded waits: a copy that never completes sets a status bit instead of
+// hanging the CTA.
+constexpr long long kTmaWaitLimit = 1LL << 22;
+constexpr int kStatusTmaTimeout = 8;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One elected thread: expect `bytes` on the barrier and start the copy of the
+// box at coordinates (c0..c3) of `map` into dst (128-byte aligned).
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            unsigned long long* bar, unsigned bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(smem_addr(dst)),
+      "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Wait for the barrier's phase `parity` to complete; false after the limit.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (long long i = 0; i < kTmaWaitLimit; ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// TMA staging of one launch: the map of the whole box's mirror (unshifted)
+// and the rows of the outermost axis that precede the launch's first row
+// (a slab of the pipelined solve); on == 0: coalesced loads instead.
+struct TmaStage {
+  const CUtensorMap* map;
+  int o_off;
+  int on;
+};
 
 // Threads of a tile's CTA: one per interface of the tile ((S+1)·P, the
 // costliest phase), rounded up to whole warps, so that no phase but the
@@ -58,10 +112,15 @@ struct Axes {
 
 // Shared-memory slab; index (la along A, lb along the pencils) is stored
 // with the x-fast index innermost so consecutive threads hit consecutive
-// banks in both orientations.
+// banks in both orientations. The state slab u is one component plane after
+// another, each plane laid out as the tensor copy writes it: along x the
+// S+4 staged cells of each of the P pencils; across x (sweeps along y or z,
+// pencils along x) S+4 rows of P+4 cells, the pencils at columns 2..P+1 (a
+// tensor copy must start at a 16-byte aligned x, 2 cells before the first
+// interior pencil).
 template <int D, int S, int P>
 struct SweepSmem {
-  float u[D + 2][(S + 4) * P];   // FP32 state slab (ghost/halo layer included)
+  alignas(128) float u[(D + 2) * (S + 4) * (P + 4)];  // FP32 state slab (ghost/halo layer included)
   float ul[D + 2][(S + 2) * P];  // face states, left / right
   float ur[D + 2][(S + 2) * P];
   float f[D + 2][(S + 1) * P];   // interface fluxes
@@ -75,8 +134,13 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
                                            const Geom& g, const Dx& dx, const double* __restrict__ dtp,
                                            float* __restrict__ acc, double* __restrict__ Unew,
                                            const FallbackQueue& q, int box,
-                                           int tA, int tB, int cC, SweepSmem<D, S, P>& sh) {
+                                           int tA, int tB, int cC, SweepSmem<D, S, P>& sh,
+                                           const TmaStage& tma, unsigned long long* bar, unsigned& parity) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
+  // component plane of the staged slab, and the index of (la, lb) in it
+  constexpr int PLANE = (A == 0) ? (S + 4) * P : (S + 4) * (P + 4);
+  auto ixu = [](int la, int lb) -> int { return (A == 0) ? lb * (S + 4) + la : la * (P + 4) + lb + 2; };
+  float* su = sh.u;
   const int NA = g.n[A];
   const int NB = (B < D) ? g.n[B] : 1;
   const int a0 = tA * S + 1;  // first interior cell of the slab along A
@@ -111,14 +175,32 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
 
   // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
-  for (int it = threadIdx.x; it < (S + 4) * P; it += TileCfg<S, P>::threads) {
-    int la, lb;
-    split(it, S + 4, la, lb);
-    const int ga = a0 - 2 + la, gb = b0 + lb;
-    const bool ok = ga <= NA + 2 && gb <= NB;
-    const long long o = ok ? offset(ga, gb) : 0;
+  if (tma.on) {
+    // one tensor copy of the whole slab (every component), zero-filled
+    // beyond the array; coordinates are array indices (Fortran index + 1)
+    if (threadIdx.x == 0) {
+      int co[3] = {0, 0, 0};
+      co[A] = a0 - 1;
+      if (B < D) co[B] = (A == 0) ? b0 + 1 : b0 - 1;
+      if (C < D) co[C] = cC + 1;
+      co[D - 1] += tma.o_off;
+      tma_load_4d(su, tma.map, co[0], co[1], co[2], 0, bar, (unsigned)((D + 2) * PLANE * sizeof(float)));
+    }
+    if (!mbar_wait(bar, parity)) {
+      atomicOr(q.status, kStatusTmaTimeout);
+      mbar_wait(bar, parity);  // let a late copy land before the smem is reused
+    }
+    parity ^= 1u;
+  } else {
+    for (int it = threadIdx.x; it < (S + 4) * P; it += TileCfg<S, P>::threads) {
+      int la, lb;
+      split(it, S + 4, la, lb);
+      const int ga = a0 - 2 + la, gb = b0 + lb;
+      const bool ok = ga <= NA + 2 && gb <= NB;
+      const long long o = ok ? offset(ga, gb) : 0;
 #pragma unroll
-    for (int c = 0; c < D + 2; ++c) sh.u[c][ix(la, lb, S + 4)] = ok ? Uf[(long long)c * F + o] : 0.f;
+      for (int c = 0; c < D + 2; ++c) su[c * PLANE + ixu(la, lb)] = ok ? Uf[(long long)c * F + o] : 0.f;
+    }
   }
   __syncthreads();
   const float dtdx = s_dtdx[0];
@@ -132,9 +214,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     float um[D + 2], u0[D + 2], up[D + 2], l[D + 2], r[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) {
-      um[c] = sh.u[c][ix(la, lb, S + 4)];
-      u0[c] = sh.u[c][ix(la + 1, lb, S + 4)];
-      up[c] = sh.u[c][ix(la + 2, lb, S + 4)];
+      um[c] = su[c * PLANE + ixu(la, lb)];
+      u0[c] = su[c * PLANE + ixu(la + 1, lb)];
+      up[c] = su[c * PLANE + ixu(la + 2, lb)];
     }
     face_states<D, A>(M.G, limiter, omega, um, u0, up, hdtdx, l, r);
 #pragma unroll
@@ -173,7 +255,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int c = 0; c < D + 2; ++c) finite = finite && isfinite(sh.u[c][ix(li + k, lb, S + 4)]);
+        for (int c = 0; c < D + 2; ++c) finite = finite && isfinite(su[c * PLANE + ixu(li + k, lb)]);
       // otherwise zero here; the FP64 correction is applied after the last
       // sweep. Each interface is queued once: by the tile whose left face it
       // is, or by the last tile for the box's right boundary.
@@ -216,15 +298,20 @@ template <int D, int A, int S, int P, int MODE>
 __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
-                 double* __restrict__ Unew, FallbackQueue q) {
+                 double* __restrict__ Unew, FallbackQueue q, const __grid_constant__ CUtensorMap map,
+                 int tma_on, int o_off) {
   constexpr int C = Axes<D, A>::C;
   __shared__ SweepSmem<D, S, P> sh;
+  __shared__ __align__(8) unsigned long long bar;
+  if (tma_on && threadIdx.x == 0) mbar_init(&bar);  // ordered by the tile's first barrier
+  unsigned parity = 0;
+  const TmaStage tma{&map, o_off, tma_on};
   // tile origin: the fast grid axis runs along x
   const int tA = (A == 0) ? blockIdx.x : blockIdx.y;
   const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
   const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
   sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, q, 0, tA, tB, cC,
-                               sh);
+                               sh, tma, &bar, parity);
 }
 
 // The same sweep over the tiles of a batch of boxes, taken from a work queue
@@ -236,6 +323,8 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
   constexpr int B = Axes<D, A>::B;
   __shared__ SweepSmem<D, S, P> sh;
   __shared__ int s_item;
+  unsigned parity = 0;
+  const TmaStage tma{nullptr, 0, 0};
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
@@ -251,7 +340,7 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
     const int tB = (int)(r % nB);
     const int cC = (int)(r / nB) + 1;
     sweep_tile<D, A, S, P, MODE>(M, b.limiter, b.omega_f, b.Uf, b.U, b.g, b.dx, b.ctl, b.acc, b.V,
-                                 q, w.box, tA, tB, cC, sh);
+                                 q, w.box, tA, tB, cC, sh, tma, nullptr, parity);
   }
 }
 

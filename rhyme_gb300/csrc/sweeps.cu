@@ -2,6 +2,8 @@
 // one dimensionality. Compiled three times (-DSWEEP_D=1, 2, 3) so the
 // instantiations (axes x candidate shapes, single box and batched) build in
 // parallel.
+#include <cstring>
+
 #include "sweep.cuh"
 
 #ifndef SWEEP_D
@@ -51,8 +53,13 @@ cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, c
   const int tA = (NA + S - 1) / S, tB = (NB + P - 1) / P;
   if ((A == 0 ? tB : tA) > 65535 || NC > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid = (A == 0) ? dim3(tA, tB, NC) : dim3(tB, tA, NC);
+  // the slab staged by one tensor copy of the whole box's mirror where
+  // possible (its coordinates along O offset by the slab's first row)
+  CUtensorMap map;
+  memset(&map, 0, sizeof map);
+  const int tma_on = encode_mirror_map(&map, Uf, g, D, A, S, P) ? 1 : 0;
   sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(
-      M, Uf + shift, U + shift, gs, dx, dtp, acc + shift, Unew + shift, qs);
+      M, Uf + shift, U + shift, gs, dx, dtp, acc + shift, Unew + shift, qs, map, tma_on, lo - 1);
   return cudaGetLastError();
 }
 

@@ -34,6 +34,7 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
            "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc", "rhyme_gpu_set_box_params",
+           "rhyme_gpu_tma_launches",
            "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
            "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
            "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
@@ -160,6 +161,7 @@ def load():
     L.rhyme_gpu_profile_steps.argtypes = [vp, C.c_int, dp, C.c_int, dp]
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
+    L.rhyme_gpu_tma_launches.argtypes = [C.POINTER(C.c_longlong)]
     L.rhyme_gpu_sweep_plan.argtypes = [vp, C.c_int, dp, ip, ip]
     L.rhyme_gpu_output_level.argtypes = [vp, ip, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_longlong]
     L.rhyme_gpu_output_wait.argtypes = [vp]
@@ -563,3 +565,12 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def tma_launches():
+    """Single-box sweep launches of this process that staged with TMA."""
+    n = C.c_longlong()
+    rc = load().rhyme_gpu_tma_launches(C.byref(n))
+    if rc != OK:
+        raise RhymeGpuError(rc, "rhyme_gpu_tma_launches")
+    return n.value

@@ -132,3 +132,18 @@ def replay(stream, base_params, courant=COURANT, hbm_budget=150 << 30, max_activ
         cu, _ = srv.stats()
     return dict(latencies=np.asarray(lat), makespan=makespan, cell_updates=cu, results=outs,
                 peak_active=peak)
+
+
+def run_alone(req, base_params, precision, courant=COURANT):
+    """The request stepped on its own (no server) in the given precision:
+    its final state array."""
+    from .params import hydro_params
+    nd = req["ndim"]
+    p = hydro_params(nd, limiter=req["limiter"], bc=req["bc"], courant=courant[nd - 1], precision=precision,
+                     gamma=base_params.get("gamma", GAMMA["monatomic"]))
+    c = req["cells"].copy()
+    with gpu.Context(p) as ctx:
+        b = ctx.register_box(c)
+        ctx.run(b, req["dx"], req["nsteps"], trace=False)
+        ctx.sync_to_host(b)
+    return c
