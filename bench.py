@@ -28,15 +28,20 @@ window sees the developed flow rather than the nearly uniform start.
 
 Other workloads (--workload): slab2d (2-D 256^2 shear slab, plain FP64,
 500 steps), riemann1d (1-D 512 cells, 100 steps), spheres3d<N>, batch4096
-(4096 uneven 3-D boxes stepped as one batch; use --steps 10) and serve (a
-seeded Poisson stream of requests served by the continuous-batching server
-against one-at-a-time plain FP64).
+(4096 uneven 3-D boxes stepped as one batch; use --steps 10), serve (a
+seeded Poisson stream of 512 requests served by the continuous-batching
+server, against one-at-a-time plain FP64 on its first 48, with per-request
+errors of the served mixed results against FP64) and rates (the GPU's FP64
+and FP32 arithmetic rates for the operations this path is bound by).
 
 --impl reference times the CPU implementation alone on the same config and
 window: the whole box, advanced by the CPU itself (with --cpu-threads N, on
 N OpenMP threads).
-Under torchrun each rank runs an independent replica (the path shards by
-box; a single box is replicated) and value is the sum over ranks.
+Under torchrun the single-box workloads run as one box in slabs along the
+outermost axis, a slab per rank, with the halo rows exchanged device to
+device over NCCL (strong scaling; --replicas: an independent replica per
+rank instead); batch4096 shards its boxes over the ranks and serve runs a
+stream per rank (weak scaling, value summed over ranks).
 """
 import argparse
 import json
@@ -519,6 +524,89 @@ def run_gpu(args, rank, local, world):
         print(json.dumps(line), flush=True)
 
 
+def run_slabs(args, rank, local, world):
+    """One box decomposed into slabs along its outermost axis, one slab per
+    rank (rhyme_gb300.slabs.run_rank: dt minimum by all-reduce, the two halo
+    rows per face exchanged device to device over NCCL). value: the whole
+    box's cell updates per second over the slowest rank's wall clock
+    (strong scaling: the box is the same at every N). e2e: the drop-in loop
+    per rank (slab upload from host memory, dt read back, ghost fill, halo
+    exchange, solve with host write-back)."""
+    import torch
+    from rhyme_gb300 import gpu, slabs
+    from rhyme_gb300.params import PERIODIC
+    torch.cuda.set_device(local)
+    cells, dx, p, cfg = workload(args.workload, args.precision)
+    ndim = p["ndim"]
+    K, W = args.steps, args.warmup
+    adv = advance_steps(args, cfg)
+    rows = slabs.split_rows(cells.shape[1] - 4, world)
+    a, c = rows[rank]
+    arr = slabs.slab_cells(cells, a, c)
+    lo_f, hi_f = 2 * (ndim - 1), 2 * (ndim - 1) + 1
+    periodic = p["bc"][lo_f] == PERIODIC and p["bc"][hi_f] == PERIODIC
+    ops = slabs.GpuOps(dx)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ctx = gpu.Context(p)
+    b = ctx.register_box(arr)
+    ctx.set_box_params(b, bc=slabs.slab_bc(p["bc"], ndim, rank, world), limiter=p["limiter"], omega=p["omega"])
+    sl = (ctx, b)
+    slabs.run_rank(sl, c, adv + W, ops, periodic, rank, world)
+    ctx.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    t_begin = time.time()
+    t0 = time.perf_counter()
+    slabs.run_rank(sl, c, K, ops, periodic, rank, world)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    el = allmax(time.perf_counter() - t0, world)
+    barrier(world)
+    clk = clocks.summary(t_begin, time.time())
+    clocks.stop()
+    value = cfg["cells"] * K / el
+    # the drop-in form: the slab's state in host memory between steps
+    ctx.sync_to_host(b)
+    ctx.set_host_writeback(b)
+    hydro_bytes = (ndim + 2) * int(np.prod(arr.shape[1:])) * 8
+
+    class DropInOps(slabs.GpuOps):
+        def dt(self, s):
+            s[0].sync_to_device(s[1])
+            return s[0].cfl_time_step(s[1], self.dx)
+
+        def solve(self, s, dt):
+            s[0].muscl_hancock_solve(s[1], self.dx, dt)
+            s[0].sync_to_host(s[1])
+
+    ke = max(1, min(K, args.e2e_steps))
+    slabs.run_rank(sl, c, min(W, 3), DropInOps(dx), periodic, rank, world)
+    windows = []
+    for _ in range(E2E_WINDOWS):
+        barrier(world)
+        t0 = time.perf_counter()
+        slabs.run_rank(sl, c, ke, DropInOps(dx), periodic, rank, world)
+        te = allmax(time.perf_counter() - t0, world)
+        windows.append(cfg["cells"] * ke / te)
+    ctx.close()
+    if rank == 0:
+        prec = cfg["precision"]
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": 1e3 * el / K, "higher_is_better": True, "scaling": "strong",
+                "vs_baseline": None, "dtype": dtype_name(prec), "data": "synthetic",
+                "config": dict(cfg, parallelism="one box in %d slabs along its outermost axis, one per GPU; "
+                                                "halo rows device to device over NCCL" % world,
+                               window=window_text(adv, W, K, cfg), slab_rows=[r[1] for r in rows],
+                               l2="inputs larger than L2 (%.2f GB of FP64 state per slab)" % (hydro_bytes / 1e9)),
+                "e2e": {"value": statistics.median(windows), "unit": METRIC, "h2d_bytes_per_step": hydro_bytes,
+                        "d2h_bytes_per_step": hydro_bytes, "windows": windows,
+                        "statistic": "median of %d windows of %d steps; bytes per rank" % (E2E_WINDOWS, ke)},
+                "clocks": clk, "gpu_launches": launches_per_step(prec, ndim) * K}
+        print(json.dumps(line), flush=True)
+
+
 def run_batch(args, rank, local, world):
     """4096 uneven 3-D boxes (edges from {8..64} per axis, Riemann or sphere
     ICs, reflective/outflow faces, van Albada) stepped as one batch: a
@@ -702,6 +790,37 @@ def run_serve(args, rank, local, world):
         print(json.dumps(line), flush=True)
 
 
+def run_rates(args, rank, local, world):
+    """Arithmetic rates of this GPU for the operations the path is bound by
+    (rhyme_gpu_rate_probe: FP64 FMA, division, square root, the restated
+    C-library pow; FP32 FMA, approximate division, exp2f(y log2f(x))),
+    CUDA events, SM clock sampled during the launches. No clock control."""
+    import torch
+    from rhyme_gb300 import gpu
+    torch.cuda.set_device(local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    rates = {}
+    t0 = time.time()
+    for k, name in enumerate(gpu.RATE_KINDS):
+        iters = 20000 if "fma" in name else 2000
+        r, ms = gpu.rate_probe(k, iters)
+        rates[name] = {"per_s": r, "ms": ms}
+    t1 = time.time()
+    clk = clocks.summary(t0, t1)
+    clocks.stop()
+    if rank == 0:
+        per = lambda n: rates[n]["per_s"]
+        line = {"metric": "operations/s", "workload": "rates", "n_gpus": 1, "rates": rates,
+                "fp32_over_fp64_fma": per("fp32_fma_flops") / per("fp64_fma_flops"),
+                "fp32_pow_over_fp64_pow": per("fp32_pow_exp2_log2") / per("fp64_pow"),
+                "clocks": clk,
+                "how": "8 independent chains per thread, 8 CTAs of 256 threads per SM, fastest of 3 launches "
+                       "after a warm-up; FMA counted as 2 flops"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -711,6 +830,10 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the other precision")
+    ap.add_argument("--slabs", action="store_true",
+                    help="the slab-decomposed form also on one GPU (one slab: the whole box)")
+    ap.add_argument("--replicas", action="store_true",
+                    help="under torchrun, step a replica of the box per rank instead of one box in slabs")
     ap.add_argument("--advance", type=int, default=None,
                     help="untimed steps before the warm-up (default: half the workload's run)")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -732,6 +855,10 @@ def main():
         run_batch(args, rank, local, world)
     elif args.workload == "serve":
         run_serve(args, rank, local, world)
+    elif args.workload == "rates":
+        run_rates(args, rank, local, world)
+    elif args.slabs or (world > 1 and not args.replicas):
+        run_slabs(args, rank, local, world)
     else:
         run_gpu(args, rank, local, world)
     if world > 1:

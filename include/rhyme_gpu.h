@@ -159,8 +159,10 @@ int rhyme_gpu_set_host_writeback(rhyme_gpu_ctx* ctx, int handle, int on);
 /*
  * Rows [row0, row0 + nrows) of the box's outermost axis (rows of the
  * ghosted block: 0 and 1 are the left ghosts, 2 .. N+1 the interior) of the
- * hydro components, device -> host into out: NDIM+2 component blocks of
- * nrows rows each, a row being the ghosted extent of the other axes. Waits.
+ * hydro components, copied into out: NDIM+2 component blocks of nrows rows
+ * each, a row being the ghosted extent of the other axes. out may be host
+ * memory or device memory (this GPU's, or a peer's with peer access), so a
+ * multi-GPU exchange can keep the rows on the devices. Waits.
  * With rhyme_gpu_set_rows, the halo exchange of a box decomposed into slabs
  * along its outermost axis (one slab per GPU): each slab sends its first and
  * last two interior rows to the neighbours' ghost rows, whose faces have the
@@ -170,7 +172,8 @@ int rhyme_gpu_set_host_writeback(rhyme_gpu_ctx* ctx, int handle, int on);
  * counterpart (the reference steps one box per process).
  */
 int rhyme_gpu_get_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, double* out);
-/* The same rows host -> device, into both state buffers of the box. */
+/* The same rows from `in` (host or device memory), into both state buffers
+ * of the box. */
 int rhyme_gpu_set_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, const double* in);
 
 /*
@@ -370,6 +373,18 @@ int rhyme_gpu_sweep_plan(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int
  * with coalesced loads and give the same results).
  */
 int rhyme_gpu_tma_launches(long long* n);
+
+/*
+ * Instrumentation (no reference counterpart): arithmetic rate of the current
+ * GPU for the operations this path is bound by, from `iters` iterations of 8
+ * independent chains per thread on 8 CTAs of 256 threads per SM (the fastest
+ * of three timed launches after one warm-up; CUDA events). kind: 0 FP64 FMA
+ * (2 flops each), 1 FP64 division, 2 FP64 square root, 3 FP64 power (the
+ * restated C-library pow), 4 FP32 FMA (2 flops), 5 FP32 approximate
+ * division, 6 FP32 power as exp2f(y log2f(x)). *ops_per_second: operations
+ * per second; *ms (optional): the timed launch.
+ */
+int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms);
 
 /*
  * No counterpart in the reference: one plain-FP64 MUSCL-Hancock update

@@ -42,6 +42,7 @@ UNITS = [
     ("kernels_output", "kernels_output.cu", []),
     ("kernels_sanity", "kernels_sanity.cu", ["--fmad=false"]),
     ("kernels_paint", "kernels_paint.cu", ["--fmad=false"]),
+    ("kernels_probe", "kernels_probe.cu", FP32_SWEEP_FLAGS),
 ]
 HEADERS = ["hydro.cuh", "rgpu_internal.h", "detmath.h", "libm_pow.h", "libm_pow_tables.h", "box_elems.cuh", "sweep.cuh"]
 

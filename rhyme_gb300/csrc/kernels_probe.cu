@@ -1,0 +1,122 @@
+// kernels_probe.cu -- arithmetic rate probe of the GPU (instrumentation).
+//
+// The roofline of this path is set by arithmetic, not by HBM: the plain FP64
+// step is bound by the FP64 pipe (divisions, square roots and the powers of
+// the exact Riemann solver), the mixed form by FP32 issue. This probe
+// measures the rates those bounds are quoted against, with the same
+// operations the solver uses: FP64 fused multiply-add, division, square
+// root and libm_pow::pow; FP32 fused multiply-add, the sweeps' approximate
+// division (this unit is built with -prec-div=false like the sweeps) and
+// their power exp2f(y log2f(x)). Every thread runs kProbeChains independent
+// dependency chains, so the pipes, not latencies, set the rate; each chain's
+// result is written out so nothing is optimised away.
+#include <cmath>
+
+#include "../../include/rhyme_gpu.h"
+#include "libm_pow.h"
+
+namespace {
+
+constexpr int kProbeChains = 8;
+constexpr int kProbeThreads = 256;
+
+template <int KIND>
+__global__ void __launch_bounds__(kProbeThreads) probe_kernel(int iters, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (KIND < 4) {
+    double v[kProbeChains];
+#pragma unroll
+    for (int c = 0; c < kProbeChains; ++c) v[c] = 1.0 + 1e-3 * (t % 97) + 1e-4 * c;
+    const double a = 0.999999, b = 1e-7, y = 0.2;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int c = 0; c < kProbeChains; ++c) {
+        if (KIND == 0) v[c] = fma(v[c], a, b);         // FP64 FMA
+        if (KIND == 1) v[c] = __ddiv_rn(1.25, v[c]);   // FP64 division (x -> 1.25/x stays near 1.1)
+        if (KIND == 2) v[c] = __dsqrt_rn(v[c] + 0.5);  // FP64 square root (converges to ~1.2)
+        if (KIND == 3) v[c] = libm_pow::pow(v[c] + 0.25, y);  // the restated C-library pow
+      }
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kProbeChains; ++c) s += v[c];
+    out[t] = s;
+  } else {
+    float v[kProbeChains];
+#pragma unroll
+    for (int c = 0; c < kProbeChains; ++c) v[c] = 1.0f + 1e-3f * (t % 97) + 1e-4f * c;
+    const float a = 0.999999f, b = 1e-7f, y = 0.2f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int c = 0; c < kProbeChains; ++c) {
+        if (KIND == 4) v[c] = fmaf(v[c], a, b);                 // FP32 FMA
+        if (KIND == 5) v[c] = 1.25f / v[c];                      // FP32 division (approximate)
+        if (KIND == 6) v[c] = exp2f(y * log2f(v[c] + 0.25f));   // FP32 power as in the sweeps
+      }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kProbeChains; ++c) s += v[c];
+    out[t] = s;
+  }
+}
+
+template <int KIND>
+cudaError_t launch_probe(int blocks, int iters, double* out, cudaStream_t st) {
+  probe_kernel<KIND><<<blocks, kProbeThreads, 0, st>>>(iters, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_kind(int kind, int blocks, int iters, double* out, cudaStream_t st) {
+  switch (kind) {
+    case 0: return launch_probe<0>(blocks, iters, out, st);
+    case 1: return launch_probe<1>(blocks, iters, out, st);
+    case 2: return launch_probe<2>(blocks, iters, out, st);
+    case 3: return launch_probe<3>(blocks, iters, out, st);
+    case 4: return launch_probe<4>(blocks, iters, out, st);
+    case 5: return launch_probe<5>(blocks, iters, out, st);
+    case 6: return launch_probe<6>(blocks, iters, out, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+extern "C" int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms) {
+  if (kind < 0 || kind > 6 || iters < 1 || !ops_per_second) return RHYME_GPU_EINVAL;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return RHYME_GPU_ECUDA;
+  const int blocks = sms * 8;  // 8 CTAs of 256 threads per SM
+  const long long threads = (long long)blocks * kProbeThreads;
+  double* out = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaMalloc((void**)&out, threads * sizeof(double));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  float best = 0.f;
+  // one warm-up launch, then the fastest of three timed launches
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    e = cudaEventRecord(ev[0], st);
+    if (e == cudaSuccess) e = launch_kind(kind, blocks, iters, out, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+    if (e == cudaSuccess && rep > 0 && (best == 0.f || t < best)) best = t;
+  }
+  if (ev[0]) cudaEventDestroy(ev[0]);
+  if (ev[1]) cudaEventDestroy(ev[1]);
+  if (st) cudaStreamDestroy(st);
+  if (out) cudaFree(out);
+  if (e != cudaSuccess || best <= 0.f) return RHYME_GPU_ECUDA;
+  // operations: one per chain step (an FMA counts as two floating-point
+  // operations for the FMA kinds)
+  const double ops = (double)threads * iters * kProbeChains * ((kind == 0 || kind == 4) ? 2.0 : 1.0);
+  *ops_per_second = ops / (best * 1e-3);
+  if (ms) *ms = best;
+  return RHYME_GPU_OK;
+}

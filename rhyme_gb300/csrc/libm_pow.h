@@ -49,7 +49,11 @@
 #include <cstdint>
 #include <cstring>
 
+#ifdef LIBM_POW_TABLES_FILE  // another coefficient set (libm_pow_calibrate.py)
+#include LIBM_POW_TABLES_FILE
+#else
 #include "libm_pow_tables.h"
+#endif
 
 #if defined(__CUDACC__)
 #define LIBM_POW_HD __host__ __device__ __forceinline__
@@ -114,7 +118,9 @@ constexpr uint64_t kSignBias = 0x800ULL << 7;  // lands on bit 63 after << 45
 constexpr double kShift = 0x1.8p52;
 
 // log of the positive normal number with bit pattern ix, as hi + *tail.
-LIBM_POW_HD double log_parts(uint64_t ix, double* tail) {
+// lo_ulps (calibration only, 0 in the library) moves the low part by that
+// many of its ulps before the final split.
+LIBM_POW_HD double log_parts(uint64_t ix, double* tail, int lo_ulps = 0) {
   const uint64_t t = ix - kOffBits;
   const int i = (int)((t >> 45) & 127);
   const int k = (int)((int64_t)t >> 52);
@@ -140,7 +146,8 @@ LIBM_POW_HD double log_parts(uint64_t ix, double* tail) {
   const double p34 = fma3(r, LIBM_POW_A4, LIBM_POW_A3);
   const double p12 = fma3(r, LIBM_POW_A2, LIBM_POW_A1);
   const double q = fma3(ar2, fma3(ar2, p56, p34), p12);
-  const double lo = fma3(ar3, q, add(add(add(lo1, lo2), lo3), lo4));
+  double lo = fma3(ar3, q, add(add(add(lo1, lo2), lo3), lo4));
+  if (lo_ulps) lo = from_bits(bits(lo) + (int64_t)lo_ulps * ((lo > 0.0) ? 1 : -1));
   const double y = add(hi, lo);
   *tail = add(sub(hi, y), lo);
   return y;
@@ -174,8 +181,13 @@ LIBM_POW_HD double exp_edge(double tmp, uint64_t sbits, uint64_t ki) {
   return mul(0x1p-1022, y);
 }
 
+// Intermediates of exp_parts for the calibration (not used by the library).
+struct ExpTrace {
+  double r, r4, u, tmp, scale;
+};
+
 // e^(x + xtail), negated when sign_bias is kSignBias.
-LIBM_POW_HD double exp_parts(double x, double xtail, uint64_t sign_bias) {
+LIBM_POW_HD double exp_parts(double x, double xtail, uint64_t sign_bias, ExpTrace* trace = nullptr) {
   uint32_t abstop = (uint32_t)(bits(x) >> 52) & 0x7ff;
   if (abstop - 0x3c9u >= 0x408u - 0x3c9u) {  // |x| < 2^-54 or |x| >= 512
     if ((int32_t)(abstop - 0x3c9u) < 0) {
@@ -198,10 +210,12 @@ LIBM_POW_HD double exp_parts(double x, double xtail, uint64_t sign_bias) {
   const double tail = from_bits(e[0]);
   const uint64_t sbits = e[1] + top;
   const double r2 = mul(r, r);
-  const double tmp = fma3(mul(r2, r2), fma3(r, LIBM_POW_C5, LIBM_POW_C4),
-                          fma3(r2, fma3(r, LIBM_POW_C3, LIBM_POW_C2), add(tail, r)));
+  const double r4 = mul(r2, r2);
+  const double u = fma3(r2, fma3(r, LIBM_POW_C3, LIBM_POW_C2), add(tail, r));
+  const double tmp = fma3(r4, fma3(r, LIBM_POW_C5, LIBM_POW_C4), u);
   if (abstop == 0) return exp_edge(tmp, sbits, ki);
   const double scale = from_bits(sbits);
+  if (trace) *trace = {r, r4, u, tmp, scale};
   return fma3(scale, tmp, scale);
 }
 

@@ -171,9 +171,10 @@ def exp_poly():
     return [float(v) for v in c]
 
 
-def calibrated(name, v):
-    """v moved by CALIBRATION[name] of its ulps (exact: stays in v's binade)."""
-    k = CALIBRATION.get(name, 0)
+def calibrated(name, v, calibration=None):
+    """v moved by calibration[name] (default CALIBRATION) of its ulps (exact:
+    stays in v's binade)."""
+    k = (CALIBRATION if calibration is None else calibration).get(name, 0)
     if not k:
         return v
     out = v + k * math.ulp(v)
@@ -185,7 +186,7 @@ def _hex(v):
     return float.hex(float(v))
 
 
-def main(out=None):
+def main(out=None, calibration=None):
     ln2 = mpmath.log(2)
     ln2_hi = _round_sig(ln2, 42)
     ln2_n = ln2 / N
@@ -216,7 +217,7 @@ def main(out=None):
     ]
     consts += [("A%d" % (k + 1), v) for k, v in enumerate(a)]
     consts += [("C%d" % (k + 2), v) for k, v in enumerate(cc)]
-    consts = [(name, calibrated(name, v)) for name, v in consts]
+    consts = [(name, calibrated(name, v, calibration)) for name, v in consts]
     for name, v in consts:
         lines.append("constexpr double LIBM_POW_%s = %s;" % (name, _hex(v)))
     lines.append("")

@@ -593,8 +593,10 @@ int rhyme_gpu_get_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, doub
   int rc = rows_geometry(ctx, b, row0, nrows, &row, &pitch);
   if (rc != RHYME_GPU_OK) return rc;
   const size_t width = (size_t)nrows * row * sizeof(double);
+  // out may be host memory or device memory (this GPU's or a peer's): the
+  // copy kind follows the pointers
   CK(cudaMemcpy2DAsync(out, width, b->state[b->cur] + (size_t)row0 * row, pitch, width, ctx->params.ndim + 2,
-                       cudaMemcpyDeviceToHost, ctx->stream));
+                       cudaMemcpyDefault, ctx->stream));
   return wait_stream(ctx);
 }
 
@@ -610,7 +612,7 @@ int rhyme_gpu_set_rows(rhyme_gpu_ctx* ctx, int handle, int row0, int nrows, cons
   const size_t off = (size_t)row0 * row;
   state_changed(b);
   CK(cudaMemcpy2DAsync(b->state[b->cur] + off, pitch, in, width, width, ctx->params.ndim + 2,
-                       cudaMemcpyHostToDevice, ctx->stream));
+                       cudaMemcpyDefault, ctx->stream));
   CK(cudaMemcpy2DAsync(b->state[1 - b->cur] + off, pitch, b->state[b->cur] + off, pitch, width,
                        ctx->params.ndim + 2, cudaMemcpyDeviceToDevice, ctx->stream));
   // the caller's buffer may be reused on return

@@ -186,8 +186,10 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
       co[D - 1] += tma.o_off;
       tma_load_4d(su, tma.map, co[0], co[1], co[2], 0, bar, (unsigned)((D + 2) * PLANE * sizeof(float)));
     }
-    if (!mbar_wait(bar, parity)) {
-      atomicOr(q.status, kStatusTmaTimeout);
+    // one warp polls the barrier; the others wait at the CTA barrier below,
+    // off the issue slots the co-resident CTAs are computing with
+    if (threadIdx.x < 32 && !mbar_wait(bar, parity)) {
+      if (threadIdx.x == 0) atomicOr(q.status, kStatusTmaTimeout);
       mbar_wait(bar, parity);  // let a late copy land before the smem is reused
     }
     parity ^= 1u;

@@ -34,7 +34,7 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
            "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc", "rhyme_gpu_set_box_params",
-           "rhyme_gpu_tma_launches",
+           "rhyme_gpu_tma_launches", "rhyme_gpu_rate_probe",
            "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
            "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
            "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
@@ -145,8 +145,8 @@ def load():
     L.rhyme_gpu_sync_to_device.argtypes = [vp, C.c_int]
     L.rhyme_gpu_sync_to_host.argtypes = [vp, C.c_int]
     L.rhyme_gpu_set_host_writeback.argtypes = [vp, C.c_int, C.c_int]
-    L.rhyme_gpu_get_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
-    L.rhyme_gpu_set_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
+    L.rhyme_gpu_get_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+    L.rhyme_gpu_set_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
     L.rhyme_gpu_cfl_time_step.argtypes = [vp, C.c_int, dp, dp]
     L.rhyme_gpu_set_boundaries.argtypes = [vp, C.c_int]
     L.rhyme_gpu_cfl_dt.argtypes = [vp, C.c_int, dp]
@@ -162,6 +162,7 @@ def load():
     L.rhyme_gpu_box_status.argtypes = [vp, C.c_int, ip]
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     L.rhyme_gpu_tma_launches.argtypes = [C.POINTER(C.c_longlong)]
+    L.rhyme_gpu_rate_probe.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.rhyme_gpu_sweep_plan.argtypes = [vp, C.c_int, dp, ip, ip]
     L.rhyme_gpu_output_level.argtypes = [vp, ip, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_longlong]
     L.rhyme_gpu_output_wait.argtypes = [vp]
@@ -309,18 +310,33 @@ class Context:
     def sync_to_host(self, box):
         self._check(self.lib.rhyme_gpu_sync_to_host(self.h, box.handle))
 
-    def get_rows(self, box, row0, nrows):
+    def rows_shape(self, box, nrows):
+        return (self.ndim + 2, int(nrows)) + box.cells.shape[2:]
+
+    def get_rows(self, box, row0, nrows, out=None):
         """Rows [row0, row0 + nrows) of the outermost axis of the box's
-        ghosted block, shape (NDIM+2, nrows, ...)."""
-        shape = (self.ndim + 2, int(nrows)) + box.cells.shape[2:]
-        out = np.empty(shape, dtype=np.float64)
-        self._check(self.lib.rhyme_gpu_get_rows(self.h, box.handle, int(row0), int(nrows), _d(out)))
+        ghosted block, shape (NDIM+2, nrows, ...): into a new host array, or
+        into `out`, a contiguous float64 torch CUDA tensor of that shape
+        (the rows then stay on the device)."""
+        if out is None:
+            out = np.empty(self.rows_shape(box, nrows), dtype=np.float64)
+            ptr = _d(out)
+        else:
+            assert out.is_cuda and out.is_contiguous() and tuple(out.shape) == self.rows_shape(box, nrows)
+            ptr = C.c_void_p(out.data_ptr())
+        self._check(self.lib.rhyme_gpu_get_rows(self.h, box.handle, int(row0), int(nrows), ptr))
         return out
 
     def set_rows(self, box, row0, rows):
-        """Writes rows (as from get_rows) at row0 into both state buffers."""
-        rows = np.ascontiguousarray(rows, dtype=np.float64)
-        self._check(self.lib.rhyme_gpu_set_rows(self.h, box.handle, int(row0), int(rows.shape[1]), _d(rows)))
+        """Writes rows (as from get_rows: a host array, or a contiguous
+        float64 torch CUDA tensor) at row0 into both state buffers."""
+        if hasattr(rows, "is_cuda") and rows.is_cuda:
+            assert rows.is_contiguous() and rows.dtype.is_floating_point and rows.element_size() == 8
+            ptr, n = C.c_void_p(rows.data_ptr()), int(rows.shape[1])
+        else:
+            rows = np.ascontiguousarray(rows, dtype=np.float64)
+            ptr, n = _d(rows), int(rows.shape[1])
+        self._check(self.lib.rhyme_gpu_set_rows(self.h, box.handle, int(row0), n, ptr))
 
     def set_host_writeback(self, box, on=True):
         """Each solve of the box also copies the new state into its cells
@@ -574,3 +590,16 @@ def tma_launches():
     if rc != OK:
         raise RhymeGpuError(rc, "rhyme_gpu_tma_launches")
     return n.value
+
+
+RATE_KINDS = ["fp64_fma_flops", "fp64_div", "fp64_sqrt", "fp64_pow", "fp32_fma_flops", "fp32_div_approx",
+              "fp32_pow_exp2_log2"]
+
+
+def rate_probe(kind, iters=2000):
+    """(operations per second, ms) of one probe kind (rhyme_gpu_rate_probe)."""
+    r, ms = C.c_double(), C.c_double()
+    rc = load().rhyme_gpu_rate_probe(int(kind), int(iters), C.byref(r), C.byref(ms))
+    if rc != OK:
+        raise RhymeGpuError(rc, "rhyme_gpu_rate_probe")
+    return r.value, ms.value

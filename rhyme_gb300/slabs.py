@@ -105,19 +105,33 @@ def run_rank(slab, count, nsteps, ops, periodic, rank, world, device=None):
     import torch
     import torch.distributed as dist
     if device is None:
-        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        device = "cuda" if world > 1 and dist.get_backend() == "nccl" else "cpu"
     dts = []
     left, right = neighbours(rank, world, periodic)
+    # rows that stay on the GPU: the library copies them straight into CUDA
+    # tensors, which NCCL sends and receives (no host staging)
+    on_device = str(device).startswith("cuda") and hasattr(ops, "rows_into")
+    if on_device and world > 1:
+        shape = ops.rows_shape(slab, GHOST)
+        first, last, into_right, into_left = (torch.empty(shape, dtype=torch.float64, device=device)
+                                              for _ in range(4))
     for _ in range(nsteps):
-        t = torch.tensor([ops.dt(slab)], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MIN)
-        dt = float(t.item())
+        if world > 1:
+            t = torch.tensor([ops.dt(slab)], dtype=torch.float64, device=device)
+            dist.all_reduce(t, op=dist.ReduceOp.MIN)
+            dt = float(t.item())
+        else:
+            dt = ops.dt(slab)
         ops.fill(slab)
         if world > 1:
-            first = torch.from_numpy(ops.get_rows(slab, GHOST, GHOST)).to(device)
-            last = torch.from_numpy(ops.get_rows(slab, count, GHOST)).to(device)
-            into_right = torch.empty_like(first)  # -> my right ghost rows
-            into_left = torch.empty_like(last)    # -> my left ghost rows
+            if on_device:
+                ops.rows_into(slab, GHOST, GHOST, first)
+                ops.rows_into(slab, count, GHOST, last)
+            else:
+                first = torch.from_numpy(ops.get_rows(slab, GHOST, GHOST)).to(device)
+                last = torch.from_numpy(ops.get_rows(slab, count, GHOST)).to(device)
+                into_right = torch.empty_like(first)  # -> my right ghost rows
+                into_left = torch.empty_like(last)    # -> my left ghost rows
             # two phases, rows travelling left then rows travelling right, so
             # that a pair of ranks (both neighbours of each other when two
             # ranks wrap around) has one message each way per phase: NCCL
@@ -131,10 +145,18 @@ def run_rank(slab, count, nsteps, ops, periodic, rank, world, device=None):
                 if reqs:
                     for q in dist.batch_isend_irecv(reqs):
                         q.wait()
-            if left is not None:
-                ops.set_rows(slab, 0, into_left.cpu().numpy())
-            if right is not None:
-                ops.set_rows(slab, count + GHOST, into_right.cpu().numpy())
+            if on_device:
+                # the receives ran on torch's stream; the library copies on its own
+                torch.cuda.current_stream().synchronize()
+                if left is not None:
+                    ops.set_rows(slab, 0, into_left)
+                if right is not None:
+                    ops.set_rows(slab, count + GHOST, into_right)
+            else:
+                if left is not None:
+                    ops.set_rows(slab, 0, into_left.cpu().numpy())
+                if right is not None:
+                    ops.set_rows(slab, count + GHOST, into_right.cpu().numpy())
         ops.solve(slab, dt)
         dts.append(dt)
     return np.array(dts)
@@ -158,6 +180,15 @@ class GpuOps:
     def get_rows(self, s, row0, n):
         ctx, box = s
         return ctx.get_rows(box, row0, n)
+
+    def rows_shape(self, s, n):
+        ctx, box = s
+        return ctx.rows_shape(box, n)
+
+    def rows_into(self, s, row0, n, out):
+        """The rows into a CUDA tensor (device to device)."""
+        ctx, box = s
+        ctx.get_rows(box, row0, n, out=out)
 
     def set_rows(self, s, row0, rows):
         ctx, box = s

@@ -57,3 +57,50 @@ def test_slabs_equal_whole_box(precision, parts, bc_z):
     assert np.array_equal(d, dref)
     for (a, c), arr in zip(rows, arrays):
         assert np.array_equal(arr[:, 2:2 + c], ref[:, 2 + a:2 + a + c])
+
+
+class DeviceRowOps(slabs.GpuOps):
+    """The halo rows through CUDA tensors (device to device), as run_rank
+    does under NCCL."""
+
+    def get_rows(self, s, row0, n):
+        import torch
+        out = torch.empty(self.rows_shape(s, n), dtype=torch.float64, device="cuda")
+        self.rows_into(s, row0, n, out)
+        return out
+
+
+def test_rows_through_cuda_tensors():
+    """get_rows into / set_rows from device memory equal the host copies."""
+    torch = pytest.importorskip("torch")
+    cells, dx, p = ic.spheres_3d(n=24, nspheres=2, seed=1)
+    with gpu.Context(dict(p, precision=FP64)) as ctx:
+        b = ctx.register_box(cells.copy())
+        host = ctx.get_rows(b, 3, 2)
+        dev = torch.empty(ctx.rows_shape(b, 2), dtype=torch.float64, device="cuda")
+        ctx.get_rows(b, 3, 2, out=dev)
+        assert np.array_equal(dev.cpu().numpy(), host)
+        ctx.set_rows(b, 0, dev * 2.0)
+        assert np.array_equal(ctx.get_rows(b, 0, 2), 2.0 * host)
+
+
+@pytest.mark.parametrize("precision", [FP64, MIXED])
+def test_slabs_with_device_rows_equal_whole_box(precision):
+    cells, dx, p = ic.spheres_3d(n=40, nspheres=5, seed=6)
+    p = dict(p, precision=precision, bc=[PERIODIC] * 6)
+    ref, dref, _ = whole(cells, dx, p, 6)
+    nz = cells.shape[1] - 4
+    rows = slabs.split_rows(nz, 3)
+    arrays = [slabs.slab_cells(cells, a, c) for a, c in rows]
+    with gpu.Context(p) as ctx:
+        ss = []
+        for r, arr in enumerate(arrays):
+            b = ctx.register_box(arr)
+            ctx.set_box_params(b, bc=slabs.slab_bc(p["bc"], 3, r, 3), limiter=p["limiter"], omega=p["omega"])
+            ss.append((ctx, b))
+        d = slabs.run_local(ss, [c for _, c in rows], 6, DeviceRowOps(dx), True)
+        for _, b in ss:
+            ctx.sync_to_host(b)
+    assert np.array_equal(d, dref)
+    for (a, c), arr in zip(rows, arrays):
+        assert np.array_equal(arr[:, 2:2 + c], ref[:, 2 + a:2 + a + c])
