@@ -164,6 +164,14 @@ __device__ __forceinline__ T limited_slope(int type, T w, T ul, T u, T ur) {
     if (r > T(0)) return r * d;
     return T(0);
   } else if (type == 3) {  // van Albada; r**2.d0 folds to r*r
+    if constexpr (sizeof(T) == sizeof(float)) {
+      // r(1+r)/(1+r^2) is 1 to float precision once r > 2^24, and beyond
+      // ~1.8e19 both products overflow and give inf/inf = NaN: take the
+      // limit. (A noise-level d_R against a resolved d_L reaches such r in
+      // the mixed form's FP32 state; the FP64 path keeps the literal form.)
+      const T phi = (r < T(1e18f)) ? r * (T(1) + r) / (T(1) + r * r) : T(1);
+      return (r > T(0)) ? fmin_ref(phi, xi_r(w, r)) * d : T(0);
+    }
     return (r > T(0)) ? fmin_ref(r * (T(1) + r) / (T(1) + r * r), xi_r(w, r)) * d : T(0);
   } else {  // superbee
     if (r > T(1)) return fmin_ref(fmin_ref(r, xi_r(w, r)), T(2)) * d;

@@ -66,15 +66,6 @@ __global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restri
 
 // |v| + cs of one cell in FP32; bad marks non-positive density or a
 // non-finite value.
-template <int D>
-__device__ __forceinline__ float speed_f32(const MixedParams& M, const float* u, int& bad) {
-  float ss = 0.f;
-#pragma unroll
-  for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
-  const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
-  if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
-  return v;
-}
 
 // Interior cell t: its FP32 mirror, written to Uf from U, and its signal
 // speed.
@@ -233,6 +224,85 @@ __global__ void __launch_bounds__(kThreads)
         }
         atomicExch(s.max_bits, 0ull);
         atomicExch(s.counter, 0u);
+      }
+    }
+  }
+}
+
+// The CFL of a step after a carrying step: dt from the carried maximum when
+// it is the current state's (no FP64 fix-up changed cells after it), else
+// the pass of cfl_f32_kernel; then the carry is cleared for this step's own
+// carrying sweep.
+template <int D>
+__global__ void __launch_bounds__(kThreads)
+    cfl_carry_kernel(MixedParams M, const double* __restrict__ U, float* __restrict__ Uf, Geom g, double courant,
+                     double mdx, StepScratch s, unsigned long long* carry_bits, int* carry_ok,
+                     const int* __restrict__ prev_fix) {
+  const bool use = *carry_ok != 0 && *prev_fix == 0;
+  if (use) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      const float mu = __uint_as_float((unsigned int)*carry_bits);
+      const double dt = courant * mdx / (double)mu;
+      *s.dt = dt;
+      if (s.dt_trace) {
+        const int pos = *s.trace_pos;
+        if (pos >= 0 && pos < s.trace_cap) s.dt_trace[pos] = dt;
+        *s.trace_pos = pos + 1;
+      }
+      *carry_bits = 0ull;
+    }
+    return;
+  }
+  const long long total = (long long)g.n[0] * g.n[1] * (long long)g.n[2];
+  float m = 0.f;
+  int bad = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const float v = signal_speed_f32<D>(M, U, Uf, g, t, bad);
+    if (v > m) m = v;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float o = __shfl_down_sync(0xffffffffu, m, off);
+    if (o > m) m = o;
+    bad |= __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  __shared__ float sm[kThreads / 32];
+  __shared__ int sb[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sm[warp] = m;
+    sb[warp] = bad;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    m = (lane < kThreads / 32) ? sm[lane] : 0.f;
+    bad = (lane < kThreads / 32) ? sb[lane] : 0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float o = __shfl_down_sync(0xffffffffu, m, off);
+      if (o > m) m = o;
+      bad |= __shfl_down_sync(0xffffffffu, bad, off);
+    }
+    if (lane == 0) {
+      atomicMax(s.max_bits, (unsigned long long)__float_as_uint(m));
+      if (bad) atomicOr(s.status, 1);
+      __threadfence();
+      const unsigned int prev = atomicAdd(s.counter, 1u);
+      if (prev == gridDim.x - 1) {
+        __threadfence();
+        const float mu = __uint_as_float((unsigned int)atomicAdd(s.max_bits, 0ull));
+        const double dt = courant * mdx / (double)mu;
+        *s.dt = dt;
+        if (s.dt_trace) {
+          const int pos = *s.trace_pos;
+          if (pos >= 0 && pos < s.trace_cap) s.dt_trace[pos] = dt;
+          *s.trace_pos = pos + 1;
+        }
+        atomicExch(s.max_bits, 0ull);
+        atomicExch(s.counter, 0u);
+        *carry_bits = 0ull;
+        *carry_ok = 1;
       }
     }
   }
@@ -433,10 +503,32 @@ cudaError_t launch_cfl_mixed(const MixedParams& M, const double* U, float* Uf, c
   return cudaGetLastError();
 }
 
+cudaError_t launch_cfl_carry(const MixedParams& M, const double* U, float* Uf, const Geom& g, double courant,
+                             const Dx& dx, const StepScratch& s, unsigned long long* carry_bits, int* carry_ok,
+                             const int* prev_fix, cudaStream_t st) {
+  const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+  int grid = grid_for(total, kThreads);
+  if (grid > 152 * 4) grid = 152 * 4;
+  switch (M.ndim) {
+    case 1:
+      cfl_carry_kernel<1><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s, carry_bits, carry_ok, prev_fix);
+      break;
+    case 2:
+      cfl_carry_kernel<2><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s, carry_bits, carry_ok, prev_fix);
+      break;
+    case 3:
+      cfl_carry_kernel<3><<<grid, kThreads, 0, st>>>(M, U, Uf, g, courant, dx.min, s, carry_bits, carry_ok, prev_fix);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
                                   double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
-                                  const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev) {
+                                  const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev,
+                                  const SweepCarry& carry) {
   // ev (optional, 3 events): recorded after the x sweep, after the y sweep
   // and at the end (the z sweep and the FP64 fix-up); absent axes record
   // at the same point.
@@ -445,7 +537,8 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
   cudaError_t e = cudaMemsetAsync(q.n, 0, sizeof(int), st);
   for (int a = 0; a < D; ++a) {
     if (e == cudaSuccess)
-      e = launch_sweep_axis(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, q, st);
+      e = launch_sweep_axis(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, q, st,
+                            a == D - 1 ? carry : SweepCarry());
     if (e == cudaSuccess && ev && a < 2) e = cudaEventRecord(ev[a], st);
   }
   for (int a = D; a < 2; ++a)

@@ -169,8 +169,38 @@ int max_cfl_blocks();
 // results).
 bool encode_mirror_map(CUtensorMap* out, const float* Uf, const Geom& g, int D, int A, int S, int P);
 
+// Signal speed |v| + cs of a cell's FP32 state (the mixed CFL's); bad is set
+// for a non-positive density or a non-finite speed, which the maximum skips.
+template <int D>
+__device__ __forceinline__ float speed_f32(const MixedParams& M, const float* u, int& bad) {
+  float ss = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) ss = ss + u[1 + a] * u[1 + a];
+  const float v = sqrtf(ss) / u[0] + sound_speed<D>(M.G, u);
+  if (!(u[0] > 0.f) || !isfinite(v)) bad = 1;
+  return v;
+}
+
+// The CFL pass carried by the last sweep of the mixed step: besides U^{n+1}
+// it writes the interior of U^{n+1}'s FP32 mirror (Uf_next) and folds the
+// FP32 signal speeds of U^{n+1} into *bits, so the next step's CFL pass
+// only forms dt (launch_cfl_carry). Null members: no carry.
+struct SweepCarry {
+  float* Uf_next = nullptr;
+  unsigned long long* bits = nullptr;
+  int* status = nullptr;
+};
+
 // Mixed-precision launchers (kernels_mixed.cu).
 cudaError_t launch_to_f32(const double* U, float* Uf, long long n, cudaStream_t st);
+// The CFL of a step whose previous step carried the pass: when *carry_ok and
+// that step queued no FP64 fix-up (*prev_fix == 0; the fix-up would have
+// changed cells after the carry), dt from *carry_bits; otherwise the whole
+// launch_cfl_mixed pass. Either way *carry_bits is cleared and *carry_ok set
+// for the step's own carrying sweep.
+cudaError_t launch_cfl_carry(const MixedParams& M, const double* U, float* Uf, const Geom& g, double courant,
+                             const Dx& dx, const StepScratch& s, unsigned long long* carry_bits, int* carry_ok,
+                             const int* prev_fix, cudaStream_t st);
 // FP32 CFL of the mixed form: also writes the interior of the FP32 mirror Uf
 // from U (the sweeps read the mirror; the step that wrote U left it stale).
 cudaError_t launch_cfl_mixed(const MixedParams& M, const double* U, float* Uf, const Geom& g, double courant,
@@ -178,7 +208,8 @@ cudaError_t launch_cfl_mixed(const MixedParams& M, const double* U, float* Uf, c
 cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const float* Uf,
                                   double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
-                                  const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr);
+                                  const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                                  const SweepCarry& carry = SweepCarry());
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 // The mixed solve of the slab of interior cells [lo, hi] of the outermost
 // axis: its sweeps, then the FP64 fix-up of the queue entries from *done on,
@@ -254,7 +285,7 @@ long long sweep_tile_count(int ndim, int axis, int shape, const int* n);
   cudaError_t launch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const float* Uf,         \
                                     const double* U, const Geom& g, const Dx& dx, const double* dtp,    \
                                     float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,   \
-                                    cudaStream_t st);                                                   \
+                                    cudaStream_t st, const SweepCarry& carry);                          \
   cudaError_t launch_batch_sweep_axis_##D(int axis, int shape, const MixedParams& M, const BoxDesc* TB, \
                                           const WorkItem* items, int n, int* head, const FallbackQueue& q, \
                                           cudaStream_t st);
@@ -266,21 +297,22 @@ RGPU_SWEEP_DECL(3)
 inline cudaError_t launch_sweep_slab(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
                                      const double* U, const Geom& g, const Dx& dx, const double* dtp,
                                      float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, const SweepCarry& carry = SweepCarry()) {
   switch (ndim) {
-    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+    case 1: return launch_sweep_axis_1(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+    case 2: return launch_sweep_axis_2(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+    case 3: return launch_sweep_axis_3(axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
     default: return cudaErrorInvalidValue;
   }
 }
 
-// The sweep over the whole box.
+// The sweep over the whole box (carry: given to the last axis only).
 inline cudaError_t launch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M, const float* Uf,
                                      const double* U, const Geom& g, const Dx& dx, const double* dtp,
-                                     float* acc, double* Unew, const FallbackQueue& q, cudaStream_t st) {
+                                     float* acc, double* Unew, const FallbackQueue& q, cudaStream_t st,
+                                     const SweepCarry& carry = SweepCarry()) {
   if (ndim < 1 || ndim > 3) return cudaErrorInvalidValue;
-  return launch_sweep_slab(ndim, axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, 1, g.n[ndim - 1], st);
+  return launch_sweep_slab(ndim, axis, shape, M, Uf, U, g, dx, dtp, acc, Unew, q, 1, g.n[ndim - 1], st, carry);
 }
 
 inline cudaError_t launch_batch_sweep_axis(int ndim, int axis, int shape, const MixedParams& M,

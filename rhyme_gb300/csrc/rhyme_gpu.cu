@@ -72,6 +72,13 @@ struct Box {
   int* fb_done = nullptr;  // fix-up entries done by the slabs solved so far
   bool mirror_valid = false;
   bool maxu_valid = false;
+  // the resident run's carry (mixed): the last sweep of each captured step
+  // writes the next state's FP32 mirror and folds its signal speeds into
+  // *carry_bits; *carry_ok (device) lets the next CFL pass use them;
+  // carry_valid: nothing changed the state since the last resident run
+  unsigned long long* carry_bits = nullptr;
+  int* carry_ok = nullptr;
+  bool carry_valid = false;
   bool wb = false;
   bool wb_pending = false;
 };
@@ -384,6 +391,7 @@ int ensure_copy_stream(rhyme_gpu_ctx* ctx) {
 void state_changed(Box* b) {
   b->mirror_valid = false;
   b->maxu_valid = false;
+  b->carry_valid = false;
   b->wb_pending = false;
 }
 
@@ -486,6 +494,8 @@ int register_box_impl(rhyme_gpu_ctx* ctx, int level, int number, double* cells, 
   b->fbq.n = (int*)(base + 32);
   b->fb_done = (int*)(base + 36);
   b->ingest_bits = (unsigned long long*)(base + 40);
+  b->carry_bits = (unsigned long long*)(base + 48);
+  b->carry_ok = (int*)(base + 56);
   b->fbq.status = b->s.status;
   b->fbq.total = b->fb_count;
   b->trace_buf = (double*)(base + 64);
@@ -765,16 +775,31 @@ int box_plan(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
 // mirror's interior), ghost fill (the FP64 state, the other buffer and the
 // mirror's ghosts), solve. Running the ghost fill on a second stream beside
 // the CFL pass made the captured step 2.8 % slower at 256^3.
+// The mixed step's carry: the last sweep writes U^{n+1}'s FP32 mirror into
+// the other buffer's mirror and folds its signal speeds.
+SweepCarry carry_of(Box* b, int cur) {
+  SweepCarry c;
+  c.Uf_next = b->Uf[1 - cur];
+  c.bits = b->carry_bits;
+  c.status = b->s.status;
+  return c;
+}
+
+// In mixed precision the step carries its CFL pass into the next one: the
+// next step's CFL pass only forms dt from the carried maximum (unless the
+// FP64 fix-up changed cells after the sweep; launch_cfl_carry).
 cudaError_t enqueue_step(rhyme_gpu_ctx* ctx, Box* b, int cur, const Dx& dx, bool trace) {
   StepScratch s = scratch_of(b, trace);
   double* U = b->state[cur];
   double* V = b->state[1 - cur];
-  cudaError_t e = ctx->mixed ? launch_cfl_mixed(b->mp, U, b->Uf[cur], b->g, b->dp.courant, dx, s, ctx->stream)
+  cudaError_t e = ctx->mixed ? launch_cfl_carry(b->mp, U, b->Uf[cur], b->g, b->dp.courant, dx, s, b->carry_bits,
+                                                b->carry_ok, b->fbq.n, ctx->stream)
                              : launch_cfl(b->dp, U, b->g, dx, s, ctx->stream);
   if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream, ctx->mixed ? b->Uf[cur] : nullptr);
   if (e != cudaSuccess) return e;
   if (ctx->mixed)
-    return launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->acc, b->g, dx, s, b->fbq, b->plan, ctx->stream);
+    return launch_mh_solve_mixed(b->mp, U, b->Uf[cur], V, b->acc, b->g, dx, s, b->fbq, b->plan, ctx->stream,
+                                 nullptr, carry_of(b, cur));
   return launch_mh_solve(b->dp, U, V, b->g, dx, s, ctx->stream);
 }
 
@@ -943,7 +968,11 @@ int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3], int nsteps
   Dx d = make_dx(ctx->params.ndim, dx);
   int rc = ensure_graphs(ctx, b, d);
   if (rc != RHYME_GPU_OK) return rc;
-  if (nsteps > 0) state_changed(b);
+  if (nsteps == 0) return RHYME_GPU_OK;
+  // a state changed since the last resident run: its first CFL pass is whole
+  if (ctx->mixed && !b->carry_valid) CK(cudaMemsetAsync(b->carry_ok, 0, sizeof(int), ctx->stream));
+  state_changed(b);
+  b->carry_valid = true;
   int done = 0;
   while (done < nsteps) {
     const int chunk = (nsteps - done < kTraceCap) ? nsteps - done : kTraceCap;
@@ -1084,6 +1113,8 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   Dx d = make_dx(ctx->params.ndim, dx);
   int prc = box_plan(ctx, b, d);
   if (prc != RHYME_GPU_OK) return prc;
+  // the step as the resident run takes it (mixed: with the carried CFL)
+  if (ctx->mixed && !b->carry_valid) CK(cudaMemsetAsync(b->carry_ok, 0, sizeof(int), ctx->stream));
   state_changed(b);
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
@@ -1096,14 +1127,16 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
     cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
     if (ctx->mixed) {
       // mixed: ms[2..4] are the x, y and z sweeps (the last one with the
-      // FP64 fix-up of the queued interfaces)
-      if (e == cudaSuccess) e = launch_cfl_mixed(b->mp, U, b->Uf[b->cur], b->g, b->dp.courant, d, sc, ctx->stream);
+      // FP64 fix-up of the queued interfaces and the carried CFL pass)
+      if (e == cudaSuccess)
+        e = launch_cfl_carry(b->mp, U, b->Uf[b->cur], b->g, b->dp.courant, d, sc, b->carry_bits, b->carry_ok,
+                             b->fbq.n, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
       if (e == cudaSuccess) e = launch_ghost_fill(b->dp, U, V, b->g, ctx->stream, b->Uf[b->cur]);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
       if (e == cudaSuccess)
         e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->acc, b->g, d, sc,
-                                  b->fbq, b->plan, ctx->stream, ev + 3);
+                                  b->fbq, b->plan, ctx->stream, ev + 3, carry_of(b, b->cur));
     } else {
       if (e == cudaSuccess) e = launch_cfl(b->dp, U, b->g, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
@@ -1125,6 +1158,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 5; ++k) ms[k] = acc[k] / nsteps;
+  b->carry_valid = ctx->mixed && rc == RHYME_GPU_OK;
   return rc;
 }
 

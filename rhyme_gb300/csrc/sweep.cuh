@@ -89,9 +89,10 @@ enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
 // and its accumulation by mode, with explicit roundings (a fused
 // multiply-add onto the running sum) so that every sweep variant performs
 // exactly the same operations.
+// Returns U^{n+1} of the component in the modes that form it (0 otherwise).
 template <int MODE>
-__device__ __forceinline__ void accumulate(float dtdx, float fl, float fr, long long oc, float* __restrict__ acc,
-                                           const double* __restrict__ U, double* __restrict__ Unew) {
+__device__ __forceinline__ double accumulate(float dtdx, float fl, float fr, long long oc, float* __restrict__ acc,
+                                             const double* __restrict__ U, double* __restrict__ Unew) {
   const float d = __fsub_rn(fl, fr);
   if (MODE == FIRST) {
     acc[oc] = __fmul_rn(dtdx, d);
@@ -99,7 +100,38 @@ __device__ __forceinline__ void accumulate(float dtdx, float fl, float fr, long 
     acc[oc] = __fmaf_rn(dtdx, d, acc[oc]);
   } else {
     const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, acc[oc]) : __fmul_rn(dtdx, d);
-    Unew[oc] = __dadd_rn(U[oc], (double)tot);
+    const double un = __dadd_rn(U[oc], (double)tot);
+    Unew[oc] = un;
+    return un;
+  }
+  return 0.0;
+}
+
+// Block-wide maximum and or of (m, bad) of a CTA of NT threads (a multiple
+// of 32), folded into *bits and *status by one thread.
+template <int NT>
+__device__ __forceinline__ void block_fold_max(float m, int bad, unsigned long long* bits, int* status) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float o = __shfl_down_sync(0xffffffffu, m, off);
+    if (o > m) m = o;
+    bad |= __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  __shared__ float sm[NT / 32];
+  __shared__ int sb[NT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sm[warp] = m;
+    sb[warp] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < NT / 32; ++k) {
+      if (sm[k] > m) m = sm[k];
+      bad |= sb[k];
+    }
+    atomicMax(bits, (unsigned long long)__float_as_uint(m));
+    if (bad) atomicOr(status, 1);
   }
 }
 
@@ -135,7 +167,8 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
                                            float* __restrict__ acc, double* __restrict__ Unew,
                                            const FallbackQueue& q, int box,
                                            int tA, int tB, int cC, SweepSmem<D, S, P>& sh,
-                                           const TmaStage& tma, unsigned long long* bar, unsigned& parity) {
+                                           const TmaStage& tma, unsigned long long* bar, unsigned& parity,
+                                           const SweepCarry& carry = SweepCarry()) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   // component plane of the staged slab, and the index of (la, lb) in it
   constexpr int PLANE = (A == 0) ? (S + 4) * P : (S + 4) * (P + 4);
@@ -282,18 +315,31 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   }
   __syncthreads();
 
-  // 4. flux differences of cells a0 .. a0+S-1 and the accumulation
+  // 4. flux differences of cells a0 .. a0+S-1 and the accumulation; with a
+  // carry (last sweep), also the FP32 mirror of U^{n+1} and its signal speed
+  constexpr bool FORMS = (MODE == LAST || MODE == ONLY);
+  const bool carrying = FORMS && carry.bits != nullptr;
+  float smax = 0.f;
+  int sbad = 0;
   for (int it = threadIdx.x; it < S * P; it += TileCfg<S, P>::threads) {
     int lu, lb;
     split(it, S, lu, lb);
     const int ga = a0 + lu, gb = b0 + lb;
     if (ga > NA || gb > NB) continue;
     const long long o = offset(ga, gb);
+    float un[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
-      accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)], (long long)c * F + o,
-                       acc, U, Unew);
+      un[c] = (float)accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
+                                      (long long)c * F + o, acc, U, Unew);
+    if (carrying) {
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c) carry.Uf_next[(long long)c * F + o] = un[c];
+      const float v = speed_f32<D>(M, un, sbad);
+      if (v > smax) smax = v;
+    }
   }
+  if (carrying) block_fold_max<TileCfg<S, P>::threads>(smax, sbad, carry.bits, carry.status);
 }
 
 template <int D, int A, int S, int P, int MODE>
@@ -301,7 +347,7 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
                  double* __restrict__ Unew, FallbackQueue q, const __grid_constant__ CUtensorMap map,
-                 int tma_on, int o_off) {
+                 int tma_on, int o_off, SweepCarry carry) {
   constexpr int C = Axes<D, A>::C;
   __shared__ SweepSmem<D, S, P> sh;
   __shared__ __align__(8) unsigned long long bar;
@@ -313,7 +359,7 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
   const int tB = (A == 0) ? blockIdx.y : blockIdx.x;
   const int cC = (C < D) ? (int)blockIdx.z + 1 : 1;
   sweep_tile<D, A, S, P, MODE>(M, M.limiter, M.omega, Uf, U, g, dx, dtp, acc, Unew, q, 0, tA, tB, cC,
-                               sh, tma, &bar, parity);
+                               sh, tma, &bar, parity, carry);
 }
 
 // The same sweep over the tiles of a batch of boxes, taken from a work queue

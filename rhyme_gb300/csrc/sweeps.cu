@@ -31,7 +31,7 @@ constexpr int mode_of() {
 template <int D, int A, int S, int P>
 cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, const Geom& g, const Dx& dx,
                        const double* dtp, float* acc, double* Unew, const FallbackQueue& q, int lo, int hi,
-                       cudaStream_t st) {
+                       cudaStream_t st, const SweepCarry& carry) {
   constexpr int B = Axes<D, A>::B, C = Axes<D, A>::C;
   constexpr int O = D - 1;
   const int NO = g.n[O];
@@ -58,8 +58,10 @@ cudaError_t launch_one(const MixedParams& M, const float* Uf, const double* U, c
   CUtensorMap map;
   memset(&map, 0, sizeof map);
   const int tma_on = encode_mirror_map(&map, Uf, g, D, A, S, P) ? 1 : 0;
+  SweepCarry cs = carry;
+  if (cs.Uf_next) cs.Uf_next += shift;
   sweep_kernel<D, A, S, P, mode_of<D, A>()><<<grid, TileCfg<S, P>::threads, 0, st>>>(
-      M, Uf + shift, U + shift, gs, dx, dtp, acc + shift, Unew + shift, qs, map, tma_on, lo - 1);
+      M, Uf + shift, U + shift, gs, dx, dtp, acc + shift, Unew + shift, qs, map, tma_on, lo - 1, cs);
   return cudaGetLastError();
 }
 
@@ -75,20 +77,20 @@ cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const Work
 template <int D, int A>
 cudaError_t by_shape(int shape, const MixedParams& M, const float* Uf, const double* U, const Geom& g,
                      const Dx& dx, const double* dtp, float* acc, double* Unew,
-                     const FallbackQueue& q, int lo, int hi, cudaStream_t st) {
+                     const FallbackQueue& q, int lo, int hi, cudaStream_t st, const SweepCarry& carry) {
   if constexpr (D == 1) {
     switch (shape) {
-      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 0: return launch_one<D, A, 64, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 1: return launch_one<D, A, 128, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 2: return launch_one<D, A, 256, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 3: return launch_one<D, A, 512, 1>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
     }
   } else {
     switch (shape) {
-      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
-      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      case 0: return launch_one<D, A, 8, 32>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 1: return launch_one<D, A, 16, 16>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 2: return launch_one<D, A, 32, 8>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
+      case 3: return launch_one<D, A, 64, 4>(M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
     }
   }
   return cudaErrorInvalidValue;
@@ -123,15 +125,16 @@ cudaError_t batch_by_shape(int shape, const MixedParams& M, const BoxDesc* TB, c
 cudaError_t RGPU_CAT(launch_sweep_axis_, SWEEP_D)(int axis, int shape, const MixedParams& M, const float* Uf,
                                                  const double* U, const Geom& g, const Dx& dx,
                                                  const double* dtp, float* acc, double* Unew,
-                                                 const FallbackQueue& q, int lo, int hi, cudaStream_t st) {
+                                                 const FallbackQueue& q, int lo, int hi, cudaStream_t st,
+                                                 const SweepCarry& carry) {
   constexpr int D = SWEEP_D;
   switch (axis) {
-    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+    case 0: return by_shape<D, 0>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
     case 1:
-      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      if constexpr (D > 1) return by_shape<D, 1>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
       break;
     case 2:
-      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st);
+      if constexpr (D > 2) return by_shape<D, 2>(shape, M, Uf, U, g, dx, dtp, acc, Unew, q, lo, hi, st, carry);
       break;
   }
   return cudaErrorInvalidValue;

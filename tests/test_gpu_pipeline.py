@@ -123,3 +123,38 @@ def test_overlapped_solve_fallback_at_slab_boundary():
     for k in range(5):
         assert np.abs(b[k] - a[k]).sum() <= 1e-12 * max(scale, np.abs(a[k]).sum()), k
     assert np.max(np.abs(db - da) / da) <= 1e-12
+
+
+@pytest.mark.parametrize("split", [[12], [5, 7], [1, 1, 10]])
+def test_resident_run_carries_the_cfl_pass(split):
+    """In mixed precision the resident run carries the CFL pass: the last
+    sweep of a step writes the next state's FP32 mirror and folds its signal
+    speeds, and the next step only forms dt from that maximum. The dts and
+    states must equal those of the step-by-step loop (whole CFL pass every
+    step) bit for bit, across run calls split anywhere and with the state
+    downloaded and uploaded again between calls (which drops the carry)."""
+    cells, dx, p = ic.spheres_3d(n=44, nspheres=5, seed=12)
+    q = dict(p, precision=MIXED)
+    a = cells.copy()
+    dts = []
+    with gpu.Context(q) as ctx:
+        box = ctx.register_box(a)
+        for k, n in enumerate(split):
+            dts.extend(ctx.run(box, dx, n))
+            if k == 1:
+                ctx.sync_to_host(box)
+                ctx.sync_to_device(box)
+        assert ctx.fallback_count(box) == 0
+        ctx.sync_to_host(box)
+    b = cells.copy()
+    ref = []
+    with gpu.Context(q) as ctx:
+        box = ctx.register_box(b)
+        for _ in range(sum(split)):
+            dt = ctx.cfl_time_step(box, dx)
+            ctx.set_boundaries(box)
+            ctx.muscl_hancock_solve(box, dx, dt)
+            ref.append(dt)
+        ctx.sync_to_host(box)
+    assert np.array_equal(np.asarray(dts), np.asarray(ref))
+    assert np.array_equal(a, b)
