@@ -61,6 +61,7 @@ METRIC = "cell-updates/s"
 L2_FLUSH_BYTES = 512 << 20
 DEFAULT_WORKLOAD = "spheres3d256"
 SERVE_REQUESTS = 512      # p99 over a stream of this many requests
+BATCH_STEPS = 200         # timed steps of the many-box workload
 SERVE_FP64_PREFIX = 48    # the one-at-a-time FP64 baseline serves this prefix
 SERVE_ERR_REQUESTS = 24   # served results replayed alone in FP64 for the error
 E2E_WINDOWS = 5
@@ -625,6 +626,9 @@ def run_batch(args, rank, local, world):
     K, W = args.steps, args.warmup
     prec = args.precision or "mixed"
     order = [prec] + ([] if args.no_compare else ["fp64" if prec == "mixed" else "mixed"])
+    # the FP64 leg's timed run is one stream wait of K x 2.3 s; the library's
+    # wait limit (600 s by default) is a guard against a hung stream
+    os.environ.setdefault("RHYME_GPU_TIMEOUT_S", str(max(600, 10 * K)))
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -755,6 +759,7 @@ def run_serve(args, rank, local, world):
         e = field_errors(served[i], ref, q["ndim"])
         fields = [names[0]] + names[1:1 + q["ndim"]] + [names[4]]
         per.append({"request": int(i), "ndim": q["ndim"], "dims": q["dims"], "steps": q["nsteps"],
+                    "fp64_finite": bool(np.isfinite(ref).all()), "served_finite": bool(np.isfinite(served[i]).all()),
                     "l1": dict(zip(fields, [x[0] for x in e])), "linf": dict(zip(fields, [x[1] for x in e]))})
     finite = [x for x in per if all(np.isfinite(v) for v in x["l1"].values())]
     errs = {"requests": len(per), "definition": "per request and field: relative L1 = sum|d|/sum|f64|, "
@@ -764,6 +769,8 @@ def run_serve(args, rank, local, world):
             "max_linf": {f: max((x["linf"].get(f, 0.0) for x in finite), default=None) for f in names},
             "median_l1_rho": float(np.median([x["l1"]["rho"] for x in finite])) if finite else None,
             "requests_over_1e-6_l1_rho": sum(1 for x in finite if x["l1"]["rho"] > 1e-6),
+            "requests_nonfinite_in_fp64": sum(1 for x in per if not x["fp64_finite"]),
+            "requests_nonfinite_in_mixed_only": sum(1 for x in per if x["fp64_finite"] and not x["served_finite"]),
             "per_request": per}
     # capacity: the same requests all submitted at once (painted on the device)
     burst = [dict(q, arrival=0.0) for q in stream]
@@ -793,7 +800,8 @@ def run_serve(args, rank, local, world):
 def run_rates(args, rank, local, world):
     """Arithmetic rates of this GPU for the operations the path is bound by
     (rhyme_gpu_rate_probe: FP64 FMA, division, square root, the restated
-    C-library pow; FP32 FMA, approximate division, exp2f(y log2f(x))),
+    C-library pow; FP32 FMA, approximate division, exp2f(y log2f(x)); the
+    FP64 add and FP64 <-> FP32 conversions of the mixed state update),
     CUDA events, SM clock sampled during the launches. No clock control."""
     import torch
     from rhyme_gb300 import gpu
@@ -804,7 +812,7 @@ def run_rates(args, rank, local, world):
     rates = {}
     t0 = time.time()
     for k, name in enumerate(gpu.RATE_KINDS):
-        iters = 20000 if "fma" in name else 2000
+        iters = 20000 if ("fma" in name or "add" in name or "conversions" in name) else 2000
         r, ms = gpu.rate_probe(k, iters)
         rates[name] = {"per_s": r, "ms": ms}
     t1 = time.time()
@@ -824,7 +832,8 @@ def run_rates(args, rank, local, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 300; 200 for batch4096, whose FP64 leg takes 2.3 s a step)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
@@ -846,6 +855,8 @@ def main():
                     help="requests of the serve workload (default %d)" % SERVE_REQUESTS)
     ap.add_argument("--rate", type=float, default=8.0)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = BATCH_STEPS if args.workload == "batch4096" else 300
     if args.warmup < 3 and args.workload != "serve":
         raise SystemExit("at least 3 warm-up steps")
     rank, local, world = dist_init()

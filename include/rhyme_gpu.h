@@ -381,8 +381,9 @@ int rhyme_gpu_tma_launches(long long* n);
  * of three timed launches after one warm-up; CUDA events). kind: 0 FP64 FMA
  * (2 flops each), 1 FP64 division, 2 FP64 square root, 3 FP64 power (the
  * restated C-library pow), 4 FP32 FMA (2 flops), 5 FP32 approximate
- * division, 6 FP32 power as exp2f(y log2f(x)). *ops_per_second: operations
- * per second; *ms (optional): the timed launch.
+ * division, 6 FP32 power as exp2f(y log2f(x)), 7 FP64 add, 8 FP64 -> FP32
+ * -> FP64 conversions (2 each). *ops_per_second: operations per second;
+ * *ms (optional): the timed launch.
  */
 int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms);
 

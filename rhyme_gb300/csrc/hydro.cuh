@@ -430,7 +430,7 @@ __device__ __forceinline__ void rp_star_right(const Gas<T>& G, const Side<D, T>&
 
 // rhyme_riemann_problem_w_kfan.f90:14-31
 template <int D, int AX, typename T>
-__device__ __noinline__ void w_kfan(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
+__device__ __forceinline__ void w_kfan_body(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
   T cs = is_right ? -s.cs : s.cs;
   const T base = G.two_gp1 + G.gm1_gp1 / cs * (s.v[AX] - dxdt);
   T prho, pp;
@@ -442,6 +442,21 @@ __device__ __noinline__ void w_kfan(const Gas<T>& G, const Side<D, T>& s, T dxdt
   v[AX] = G.two_gp1 * (cs + G.half_gm1 * s.v[AX] + dxdt);
   T p = s.p * pp;
   prim_vars_to_cons<D>(G, rho, v, p, u);
+}
+
+template <int D, int AX, typename T>
+__device__ __noinline__ void w_kfan_call(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
+  w_kfan_body<D, AX>(G, s, dxdt, is_right, u);
+}
+
+// The double form is a call (its powers are long and rarely sampled); the
+// float form is inlined: a call would keep the caller's state vector in
+// local memory (its address escapes), a load and store per component on
+// every interface of the FP32 sweeps.
+template <int D, int AX, typename T>
+__device__ __forceinline__ void w_kfan(const Gas<T>& G, const Side<D, T>& s, T dxdt, bool is_right, T* u) {
+  if constexpr (sizeof(T) == sizeof(float)) w_kfan_body<D, AX>(G, s, dxdt, is_right, u);
+  else w_kfan_call<D, AX>(G, s, dxdt, is_right, u);
 }
 
 // rhyme_riemann_problem_w_star{L,R}_{sho,fan}.f90:12-15

@@ -7,7 +7,8 @@
 // operations the solver uses: FP64 fused multiply-add, division, square
 // root and libm_pow::pow; FP32 fused multiply-add, the sweeps' approximate
 // division (this unit is built with -prec-div=false like the sweeps) and
-// their power exp2f(y log2f(x)). Every thread runs kProbeChains independent
+// their power exp2f(y log2f(x)); and the two FP64 operations of the mixed
+// form's state update, the FP64 add and the FP64 <-> FP32 conversions. Every thread runs kProbeChains independent
 // dependency chains, so the pipes, not latencies, set the rate; each chain's
 // result is written out so nothing is optimised away.
 #include <cmath>
@@ -23,7 +24,7 @@ constexpr int kProbeThreads = 256;
 template <int KIND>
 __global__ void __launch_bounds__(kProbeThreads) probe_kernel(int iters, double* out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (KIND < 4) {
+  if (KIND < 4 || KIND >= 7) {
     double v[kProbeChains];
 #pragma unroll
     for (int c = 0; c < kProbeChains; ++c) v[c] = 1.0 + 1e-3 * (t % 97) + 1e-4 * c;
@@ -35,6 +36,10 @@ __global__ void __launch_bounds__(kProbeThreads) probe_kernel(int iters, double*
         if (KIND == 1) v[c] = __ddiv_rn(1.25, v[c]);   // FP64 division (x -> 1.25/x stays near 1.1)
         if (KIND == 2) v[c] = __dsqrt_rn(v[c] + 0.5);  // FP64 square root (converges to ~1.2)
         if (KIND == 3) v[c] = libm_pow::pow(v[c] + 0.25, y);  // the restated C-library pow
+        if (KIND == 7) v[c] = __dadd_rn(v[c], b);               // FP64 add
+        // FP64 -> FP32 -> FP64 (two conversions; the FP32 multiply keeps
+        // the chain from folding)
+        if (KIND == 8) v[c] = (double)__fmul_rn(__double2float_rn(v[c]), 0.9999999f);
       }
     }
     double s = 0.0;
@@ -76,6 +81,8 @@ cudaError_t launch_kind(int kind, int blocks, int iters, double* out, cudaStream
     case 4: return launch_probe<4>(blocks, iters, out, st);
     case 5: return launch_probe<5>(blocks, iters, out, st);
     case 6: return launch_probe<6>(blocks, iters, out, st);
+    case 7: return launch_probe<7>(blocks, iters, out, st);
+    case 8: return launch_probe<8>(blocks, iters, out, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -83,7 +90,7 @@ cudaError_t launch_kind(int kind, int blocks, int iters, double* out, cudaStream
 }  // namespace
 
 extern "C" int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms) {
-  if (kind < 0 || kind > 6 || iters < 1 || !ops_per_second) return RHYME_GPU_EINVAL;
+  if (kind < 0 || kind > 8 || iters < 1 || !ops_per_second) return RHYME_GPU_EINVAL;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -114,8 +121,9 @@ extern "C" int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second,
   if (out) cudaFree(out);
   if (e != cudaSuccess || best <= 0.f) return RHYME_GPU_ECUDA;
   // operations: one per chain step (an FMA counts as two floating-point
-  // operations for the FMA kinds)
-  const double ops = (double)threads * iters * kProbeChains * ((kind == 0 || kind == 4) ? 2.0 : 1.0);
+  // operations for the FMA kinds, the conversion kind two conversions)
+  const double ops =
+      (double)threads * iters * kProbeChains * ((kind == 0 || kind == 4 || kind == 8) ? 2.0 : 1.0);
   *ops_per_second = ops / (best * 1e-3);
   if (ms) *ms = best;
   return RHYME_GPU_OK;

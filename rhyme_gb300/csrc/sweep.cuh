@@ -69,6 +69,19 @@ struct TmaStage {
   int on;
 };
 
+// Asynchronous 4- and 8-byte copies global -> shared (cp.async), completed
+// per thread by cp_async_wait_all: the accumulator and the FP64 state a tile
+// adds to at its end are fetched when the tile starts, behind the staging
+// and the Riemann problems.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Threads of a tile's CTA: one per interface of the tile ((S+1)·P, the
 // costliest phase), rounded up to whole warps, so that no phase but the
 // shared-memory staging needs a second, mostly idle round behind a barrier;
@@ -88,19 +101,20 @@ enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
 // The flux difference dt/dx (F_left - F_right) of one component of one cell
 // and its accumulation by mode, with explicit roundings (a fused
 // multiply-add onto the running sum) so that every sweep variant performs
-// exactly the same operations.
+// exactly the same operations. a_prev / u_prev: the component's accumulator
+// (MID, LAST) and U^n (LAST, ONLY), prefetched.
 // Returns U^{n+1} of the component in the modes that form it (0 otherwise).
 template <int MODE>
-__device__ __forceinline__ double accumulate(float dtdx, float fl, float fr, long long oc, float* __restrict__ acc,
-                                             const double* __restrict__ U, double* __restrict__ Unew) {
+__device__ __forceinline__ double accumulate(float dtdx, float fl, float fr, float a_prev, double u_prev,
+                                             long long oc, float* __restrict__ acc, double* __restrict__ Unew) {
   const float d = __fsub_rn(fl, fr);
   if (MODE == FIRST) {
     acc[oc] = __fmul_rn(dtdx, d);
   } else if (MODE == MID) {
-    acc[oc] = __fmaf_rn(dtdx, d, acc[oc]);
+    acc[oc] = __fmaf_rn(dtdx, d, a_prev);
   } else {
-    const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, acc[oc]) : __fmul_rn(dtdx, d);
-    const double un = __dadd_rn(U[oc], (double)tot);
+    const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, a_prev) : __fmul_rn(dtdx, d);
+    const double un = __dadd_rn(u_prev, (double)tot);
     Unew[oc] = un;
     return un;
   }
@@ -179,14 +193,17 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   const int a0 = tA * S + 1;  // first interior cell of the slab along A
   const int b0 = tB * P + 1;
   const long long F = g.field;
-  // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on GB300)
+  // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on
+  // GB300), formed by a thread outside the warp that issues and polls the
+  // staging copy, while the copy is in flight
   __shared__ float s_dtdx[2];
+  constexpr int kDtThread = TileCfg<S, P>::threads > 32 ? 32 : 0;
+  // the accumulator (MID, LAST) and U^n (LAST, ONLY) of the tile's cells
+  constexpr bool PRE_ACC = (MODE == MID || MODE == LAST);
+  constexpr bool PRE_U = (MODE == LAST || MODE == ONLY);
+  __shared__ float pre_acc[PRE_ACC ? (D + 2) * S * P : 1];
+  __shared__ double pre_u[PRE_U ? (D + 2) * S * P : 1];
   __syncthreads();  // the previous tile of this CTA is done with the smem
-  if (threadIdx.x == 0) {
-    const double dt = *dtp;
-    s_dtdx[0] = (float)(dt / dx.v[A]);
-    s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
-  }
 
   auto offset = [&](int ga, int gb) -> long long {
     int c3[3] = {1, 1, 1};
@@ -207,6 +224,23 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   };
   auto ix = [&](int la, int lb, int na) -> int { return (A == 0) ? lb * na + la : la * P + lb; };
 
+  // 0. start the copies of the accumulator and U^n of the tile's cells
+  if (PRE_ACC || PRE_U) {
+    for (int it = threadIdx.x; it < S * P; it += TileCfg<S, P>::threads) {
+      int lu, lb;
+      split(it, S, lu, lb);
+      const int ga = a0 + lu, gb = b0 + lb;
+      if (ga > NA || gb > NB) continue;
+      const long long o = offset(ga, gb);
+#pragma unroll
+      for (int c = 0; c < D + 2; ++c) {
+        if (PRE_ACC) cp_async4(&pre_acc[c * S * P + it], &acc[(long long)c * F + o]);
+        if (PRE_U) cp_async8(&pre_u[c * S * P + it], &U[(long long)c * F + o]);
+      }
+    }
+    cp_async_commit();
+  }
+
   // 1. stage the FP32 slab: cells a0-2 .. a0+S+1 along A
   if (tma.on) {
     // one tensor copy of the whole slab (every component), zero-filled
@@ -219,6 +253,11 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
       co[D - 1] += tma.o_off;
       tma_load_4d(su, tma.map, co[0], co[1], co[2], 0, bar, (unsigned)((D + 2) * PLANE * sizeof(float)));
     }
+    if (threadIdx.x == kDtThread) {
+      const double dt = *dtp;
+      s_dtdx[0] = (float)(dt / dx.v[A]);
+      s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+    }
     // one warp polls the barrier; the others wait at the CTA barrier below,
     // off the issue slots the co-resident CTAs are computing with
     if (threadIdx.x < 32 && !mbar_wait(bar, parity)) {
@@ -227,6 +266,11 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     }
     parity ^= 1u;
   } else {
+    if (threadIdx.x == kDtThread) {
+      const double dt = *dtp;
+      s_dtdx[0] = (float)(dt / dx.v[A]);
+      s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+    }
     for (int it = threadIdx.x; it < (S + 4) * P; it += TileCfg<S, P>::threads) {
       int la, lb;
       split(it, S + 4, la, lb);
@@ -327,11 +371,13 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     const int ga = a0 + lu, gb = b0 + lb;
     if (ga > NA || gb > NB) continue;
     const long long o = offset(ga, gb);
+    if (PRE_ACC || PRE_U) cp_async_wait_all();  // this thread's copies (same items as phase 0)
     float un[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
       un[c] = (float)accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
-                                      (long long)c * F + o, acc, U, Unew);
+                                      PRE_ACC ? pre_acc[c * S * P + it] : 0.f, PRE_U ? pre_u[c * S * P + it] : 0.0,
+                                      (long long)c * F + o, acc, Unew);
     if (carrying) {
 #pragma unroll
       for (int c = 0; c < D + 2; ++c) carry.Uf_next[(long long)c * F + o] = un[c];

@@ -593,7 +593,7 @@ def tma_launches():
 
 
 RATE_KINDS = ["fp64_fma_flops", "fp64_div", "fp64_sqrt", "fp64_pow", "fp32_fma_flops", "fp32_div_approx",
-              "fp32_pow_exp2_log2"]
+              "fp32_pow_exp2_log2", "fp64_add", "fp64_fp32_conversions"]
 
 
 def rate_probe(kind, iters=2000):

@@ -6,12 +6,12 @@ Not a pytest module (the oracle needs about five minutes per 300-step run on
     python tests/parity_full.py [--n 256] [--steps 300]
 
 It steps the box on the GPU in plain FP64 and in mixed precision, and on the
-CPU with the oracle twice: with the deterministic power both sides share
-(where the FP64 GPU result must be bit-identical) and with the C library's
-pow, the arithmetic of the compiled reference. It prints one JSON object:
-per field relative L1 / Linf of each GPU form against each oracle run, the
-largest relative dt difference and whether the FP64 GPU run is bit-identical
-to the deterministic-power oracle.
+CPU with the oracle, whose powers are the C library's pow (the arithmetic of
+the compiled reference); the GPU's FP64 kernels raise powers with a
+restatement of that pow, so the FP64 run must be bit-identical. It prints
+one JSON object: per field relative L1 / Linf of each GPU form against the
+oracle, the largest relative dt difference, whether the FP64 GPU run is
+bit-identical to the oracle, and mixed against FP64 on the GPU.
 """
 import argparse
 import json

@@ -33,7 +33,8 @@ def test_c_driver_runs_on_the_gpu(tmp_path):
     assert out.returncode == 0, out.stderr
     run = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert run.returncode == 0, run.stderr
-    words = run.stdout.split()
+    # "mass M0 -> M1, last dt DT"
+    words = run.stdout.replace(",", " ").split()
     m0, m1, dt = float(words[1]), float(words[3]), float(words[6])
     assert abs(m1 - m0) <= 1e-13 * m0 and dt > 0.0
 
