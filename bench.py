@@ -608,6 +608,37 @@ def run_slabs(args, rank, local, world):
         print(json.dumps(line), flush=True)
 
 
+def trace_mixed_only(items, idx, nsteps, physical):
+    """Each box that ends unphysical in mixed precision only, stepped alone in
+    FP64 (the batch's FP64 result bit for bit) and in mixed precision with
+    the state checked after every step: the first unphysical step of each,
+    and how many such boxes stay physical at every FP64 step (a mixed-only
+    loss) or pass through an unphysical FP64 state that later recovers."""
+    from rhyme_gb300 import gpu
+    from rhyme_gb300.params import FP64, MIXED
+    first = {"fp64": [], "mixed": []}
+    for i in idx:
+        c0, dx, p = items[i]
+        for name, prec in (("fp64", FP64), ("mixed", MIXED)):
+            c = c0.copy()
+            step = None
+            with gpu.Context(dict(p, precision=prec)) as ctx:
+                b = ctx.register_box(c)
+                for s in range(nsteps):
+                    ctx.run(b, dx, 1)
+                    ctx.sync_to_host(b)
+                    if not physical(c[:, 2:-2, 2:-2, 2:-2]):
+                        step = s + 1
+                        break
+            first[name].append(step)
+    lost = sum(1 for f in first["fp64"] if f is None)
+    return {"boxes": len(idx), "fp64_physical_at_every_step": lost,
+            "fp64_unphysical_at_some_step": len(idx) - lost,
+            "mixed_unphysical_before_fp64": sum(1 for f, m in zip(first["fp64"], first["mixed"])
+                                                if m is not None and (f is None or m < f)),
+            "first_unphysical_step": {"fp64": first["fp64"], "mixed": first["mixed"]}}
+
+
 def run_batch(args, rank, local, world):
     """4096 uneven 3-D boxes (edges from {8..64} per axis, Riemann or sphere
     ICs, reflective/outflow faces, van Albada) stepped as one batch: a
@@ -680,7 +711,8 @@ def run_batch(args, rank, local, world):
             ke = 0.5 * (c[1] ** 2 + c[2] ** 2 + c[3] ** 2) / c[0]
             return bool(((c[4] - ke) * (2.0 / 3.0)).min() > 0)
 
-        for x, y in zip(a, b):
+        mixed_only = []
+        for i, (x, y) in enumerate(zip(a, b)):
             xi, yi = x[:, 2:-2, 2:-2, 2:-2], y[:, 2:-2, 2:-2, 2:-2]
             ok64 = physical(yi)
             okm = physical(xi)
@@ -689,6 +721,7 @@ def run_batch(args, rank, local, world):
                 continue
             if not okm:
                 bad_mixed_only += 1
+                mixed_only.append(i)
                 continue
             used += 1
             d = np.abs(xi - yi).reshape(5, -1)
@@ -698,10 +731,12 @@ def run_batch(args, rank, local, world):
             dm = np.maximum(dm, d.max(1))
             sm = np.maximum(sm, r.max(1))
         names = ["rho", "rho_vx", "rho_vy", "rho_vz", "e_tot"]
+        traces = trace_mixed_only(items, mixed_only, W + K, physical)
         cmp = {"after_steps": W + K, "definition": "relative L1 = sum|d|/sum|f64|, relative Linf = "
                "max|d|/max|f64| over the interiors of the boxes whose FP64 state after the run is "
                "physical (finite, positive density and pressure)", "boxes_compared": used,
                "boxes_failing_in_fp64": bad64, "boxes_failing_in_mixed_only": bad_mixed_only,
+               "mixed_only_boxes_traced": traces,
                "l1": dict(zip(names, (d1 / s1).tolist())), "linf": dict(zip(names, (dm / sm).tolist()))}
     if rank == 0:
         h = res[prec]

@@ -26,8 +26,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # CPU oracle operation for operation; the mixed-precision units keep it.
 # The FP32 arithmetic of the mixed form (sweeps, CFL) uses the hardware's
 # approximate FP32 division and square root (<= 2 ulp) instead of the
-# IEEE-exact sequences; FP64 arithmetic is unaffected by these flags.
-FP32_SWEEP_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
+# IEEE-exact sequences, with FP32 subnormals flushed to zero (the state's
+# FP32 values are far above 1e-38; mirrors are flushed alike in every unit,
+# rgpu_internal.h mirror_of); FP64 arithmetic is unaffected by these flags.
+FP32_SWEEP_FLAGS = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 
 UNITS = [
     ("kernels_box", "kernels_box.cu", ["--fmad=false"]),

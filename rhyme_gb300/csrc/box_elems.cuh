@@ -120,8 +120,8 @@ __device__ __forceinline__ void ghost_elem(const BoxRules& R, T* __restrict__ U,
     }
     if (Mf) {
       float* m = Mf + (long long)c * g.field;
-      m[g0] = (float)f[g0];
-      m[g1] = (float)f[g1];
+      m[g0] = mirror_of(f[g0]);
+      m[g1] = mirror_of(f[g1]);
     }
   }
 }

@@ -286,31 +286,48 @@ __device__ __forceinline__ void nonlinear_wave(const Gas<T>& G, WaveSide<T>& w, 
   }
 }
 
+// Guess 0 of rhyme_irs_guess_p_star.f90:14-38 (the adaptive PVRS /
+// two-rarefaction / two-shock choice), not yet floored.
+template <typename T>
+__device__ __forceinline__ T guess_p_star_adaptive(const Gas<T>& G, T l_rho, T vl, T l_p, T l_cs, T r_rho, T vr,
+                                                   T r_p, T r_cs) {
+  T p;
+  const T q_user = T(2);
+  T cup = T(0.25) * (l_rho + r_rho) * (l_cs + r_cs);
+  T ppv = fmax_ref(T(0.5) * (l_p + r_p) + T(0.5) * (vl - vr) * cup, T(0));
+  T p_min = fmin_ref(l_p, r_p);
+  T p_max = fmax_ref(l_p, r_p);
+  T q_max = p_max / p_min;
+  if (q_max <= q_user && (p_min < ppv && ppv < p_max)) {
+    p = ppv;  // PVRS
+  } else if (ppv < p_min) {  // two-rarefaction
+    T pq = m_pow(l_p / r_p, G.gm1_2g);
+    T um = (pq * vl / l_cs + vr / r_cs + G.two_gm1 * (pq - T(1))) / (pq / l_cs + T(1) / r_cs);
+    T ptl = T(1) + G.half_gm1 * (vl - um) / l_cs;
+    T ptr = T(1) + G.half_gm1 * (um - vr) / r_cs;
+    p = T(0.5) * (l_p * m_pow(ptl, G.inv_gm1_2g) + r_p * m_pow(ptr, G.inv_gm1_2g));
+  } else {  // two-shock
+    T gel = m_sqrt((G.two_gp1 / l_rho) / (G.gm1_gp1 * l_p + ppv));
+    T ger = m_sqrt((G.two_gp1 / r_rho) / (G.gm1_gp1 * r_p + ppv));
+    p = (gel * l_p + ger * r_p - (vr - vl)) / (gel + ger);
+  }
+  return p;
+}
+
+// Guess 0, floored at tiny, inlined (the mixed form's FP32 solve).
+template <typename T>
+__device__ __forceinline__ T guess_p_star_first(const Gas<T>& G, T l_rho, T vl, T l_p, T l_cs, T r_rho, T vr,
+                                                T r_p, T r_cs) {
+  return fmax_ref(guess_p_star_adaptive(G, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs), Limits<T>::tiny());
+}
+
 // Guess number k (0..5) of rhyme_irs_guess_p_star.f90:14-71, floored at tiny.
 template <typename T>
 __device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T l_p, T l_cs, T r_rho,
                                        T vr, T r_p, T r_cs) {
   T p;
   if (k == 0) {
-    const T q_user = T(2);
-    T cup = T(0.25) * (l_rho + r_rho) * (l_cs + r_cs);
-    T ppv = fmax_ref(T(0.5) * (l_p + r_p) + T(0.5) * (vl - vr) * cup, T(0));
-    T p_min = fmin_ref(l_p, r_p);
-    T p_max = fmax_ref(l_p, r_p);
-    T q_max = p_max / p_min;
-    if (q_max <= q_user && (p_min < ppv && ppv < p_max)) {
-      p = ppv;  // PVRS
-    } else if (ppv < p_min) {  // two-rarefaction
-      T pq = m_pow(l_p / r_p, G.gm1_2g);
-      T um = (pq * vl / l_cs + vr / r_cs + G.two_gm1 * (pq - T(1))) / (pq / l_cs + T(1) / r_cs);
-      T ptl = T(1) + G.half_gm1 * (vl - um) / l_cs;
-      T ptr = T(1) + G.half_gm1 * (um - vr) / r_cs;
-      p = T(0.5) * (l_p * m_pow(ptl, G.inv_gm1_2g) + r_p * m_pow(ptr, G.inv_gm1_2g));
-    } else {  // two-shock
-      T gel = m_sqrt((G.two_gp1 / l_rho) / (G.gm1_gp1 * l_p + ppv));
-      T ger = m_sqrt((G.two_gp1 / r_rho) / (G.gm1_gp1 * r_p + ppv));
-      p = (gel * l_p + ger * r_p - (vr - vl)) / (gel + ger);
-    }
+    p = guess_p_star_adaptive(G, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
   } else if (k == 1) {  // Ramses
     p = (r_rho * r_cs * l_p + l_rho * l_cs * r_p + r_cs * l_cs * (l_rho * vl - r_rho * vr)) /
         (r_rho * r_cs + l_rho * l_cs);
@@ -362,6 +379,35 @@ __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rh
   return p_star;
 }
 
+// The first guess's Newton iteration alone (the mixed form's FP32 solve):
+// the same operations as irs_exec's first pass, inlined, with the later
+// guesses left out. An interface whose first guess does not meet the
+// tolerance is redone in FP64 (rp_solve with CHECK), so this returns the
+// same p* as irs_exec wherever its result is used.
+template <typename T>
+__device__ __forceinline__ T irs_exec_first(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
+                                            T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f, bool* converged) {
+  T l_fp, r_fp;
+  *converged = false;
+  WaveSide<T> WL = wave_side<T, false>(G, l_rho, l_p, l_cs);
+  WaveSide<T> WR = wave_side<T, false>(G, r_rho, r_p, r_cs);
+  T p_star = guess_p_star_first(G, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
+  T p_prev = p_star;
+  for (int i = 1; i <= n_iter; ++i) {
+    nonlinear_wave<T, false>(G, WL, p_star, l_f, l_fp);
+    nonlinear_wave<T, false>(G, WR, p_star, r_f, r_fp);
+    p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
+    if (p_star < T(0)) break;
+    if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) {
+      *converged = true;
+      break;
+    }
+    p_prev = p_star;
+  }
+  if (p_star < T(0)) p_star = T(0);
+  return p_star;
+}
+
 // rp_side_t (rhyme_riemann_problem.f90:53-56)
 template <int D, typename T>
 struct Side {
@@ -383,11 +429,15 @@ struct Star {
 // sampling reads is formed: p* and u* (:12-38), then the left (:40, 43-53)
 // or the right (:41, 55-65) star state, each with the reference's
 // operations.
-template <int D, int AX, typename T, bool LAZY>
+template <int D, int AX, typename T, bool LAZY, bool FIRST_ONLY = false>
 __device__ __forceinline__ void rp_star_pu(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
                                            const Side<D, T>& R, Star<T>& s) {
-  s.p = irs_exec<T, LAZY>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
-                 s.r_f, &s.converged);
+  if constexpr (FIRST_ONLY)
+    s.p = irs_exec_first<T>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
+                            s.r_f, &s.converged);
+  else
+    s.p = irs_exec<T, LAZY>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
+                            s.r_f, &s.converged);
   if (s.p < rp.vac_p) s.p = rp.vac_p;
   s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
 }
@@ -601,7 +651,9 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       }
     } else {
       Star<T> s;
-      rp_star_pu<D, AX, T, LAZY>(G, rp, L, R, s);
+      // with CHECK, an interface whose first guess misses is redone in FP64:
+      // the later guesses are never used
+      rp_star_pu<D, AX, T, LAZY, CHECK>(G, rp, L, R, s);
       if (CHECK && !s.converged) {
         *need64 = true;
         return;

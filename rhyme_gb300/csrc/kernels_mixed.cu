@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kThreads) to_f32_kernel(const double* __restri
                                                           float* __restrict__ Uf, long long n) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x)
-    Uf[t] = (float)U[t];
+    Uf[t] = mirror_of(U[t]);
 }
 
 // |v| + cs of one cell in FP32; bad marks non-positive density or a
@@ -81,7 +81,7 @@ __device__ __forceinline__ float signal_speed_f32(const MixedParams& M, const do
   float u[D + 2];
 #pragma unroll
   for (int c = 0; c < D + 2; ++c) {
-    u[c] = (float)U[(long long)c * g.field + o];
+    u[c] = mirror_of(U[(long long)c * g.field + o]);
     Uf[(long long)c * g.field + o] = u[c];
   }
   return speed_f32<D>(M, u, bad);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) {
       const double x = U[(long long)c * F + t];
-      u[c] = (float)x;
+      u[c] = mirror_of(x);
       Uf[(long long)c * F + t] = u[c];
       if (!in) V[(long long)c * F + t] = x;
     }

@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int c = 0; c < K; ++c) {
       U[(long long)c * g.field + o] = u[c];
-      if (Uf) Uf[(long long)c * g.field + o] = (float)u[c];
+      if (Uf) Uf[(long long)c * g.field + o] = mirror_of(u[c]);
     }
   }
 }

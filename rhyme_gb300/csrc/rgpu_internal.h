@@ -169,6 +169,16 @@ int max_cfl_blocks();
 // results).
 bool encode_mirror_map(CUtensorMap* out, const float* Uf, const Geom& g, int D, int A, int S, int P);
 
+// The FP32 mirror of an FP64 state value: rounded to nearest, an FP32
+// subnormal flushed to zero of the same sign. The FP32 units of the mixed
+// form run with denormals flushed (-ftz=true) and the others do not; the
+// explicit flush gives every unit that writes a mirror (CFL pass, carried
+// pass, ghost fill, ingest, painting) the same bits.
+__device__ __forceinline__ float mirror_of(double x) {
+  const float f = __double2float_rn(x);
+  return (fabsf(f) < FLT_MIN) ? copysignf(0.f, f) : f;
+}
+
 // Signal speed |v| + cs of a cell's FP32 state (the mixed CFL's); bad is set
 // for a non-positive density or a non-finite speed, which the maximum skips.
 template <int D>

@@ -375,9 +375,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     float un[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
-      un[c] = (float)accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
+      un[c] = mirror_of(accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
                                       PRE_ACC ? pre_acc[c * S * P + it] : 0.f, PRE_U ? pre_u[c * S * P + it] : 0.0,
-                                      (long long)c * F + o, acc, Unew);
+                                      (long long)c * F + o, acc, Unew));
     if (carrying) {
 #pragma unroll
       for (int c = 0; c < D + 2; ++c) carry.Uf_next[(long long)c * F + o] = un[c];
