@@ -388,6 +388,15 @@ int rhyme_gpu_tma_launches(long long* n);
 int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms);
 
 /*
+ * Instrumentation (no reference counterpart): checks the integer forms of
+ * the FP64 <-> FP32 conversions of the mixed state update against the
+ * hardware conversions on n pseudo-random values from `seed` (doubles of
+ * every exponent, FP32 rounding ties and range limits, FP32 values).
+ * *mismatches: the number that differ (0 expected).
+ */
+int rhyme_gpu_check_conversions(long long n, unsigned long long seed, unsigned long long* mismatches);
+
+/*
  * No counterpart in the reference: one plain-FP64 MUSCL-Hancock update
  * (the same kernels as rhyme_gpu_mh_solve) that allocates nothing, for
  * callers that cannot allocate device memory: hosts whose device arrays come

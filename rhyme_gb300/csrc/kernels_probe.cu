@@ -15,6 +15,7 @@
 
 #include "../../include/rhyme_gpu.h"
 #include "libm_pow.h"
+#include "rgpu_internal.h"
 
 namespace {
 
@@ -87,7 +88,73 @@ cudaError_t launch_kind(int kind, int blocks, int iters, double* out, cudaStream
   return cudaErrorInvalidValue;
 }
 
+// Self-check of the integer conversions of the mixed state update
+// (rgpu_internal.h widen_f32, narrow_mirror) against the hardware ones, on
+// n pseudo-random bit patterns per thread family (splitmix64): doubles of
+// every exponent, doubles near the FP32 rounding boundaries, ties, the
+// limits of the FP32 range, and FP32 values (subnormals excluded: the FP32
+// units flush them).
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void conversion_check_kernel(long long n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long local = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long s = seed ^ (unsigned long long)t * 0xD1B54A32D192ED03ull;
+    const unsigned long long r = splitmix(s);
+    unsigned long long bits;
+    switch (t & 3) {
+      case 0: bits = r; break;  // any double
+      case 1: {                 // FP32 exponent range, low bits at or next to a tie
+        const unsigned long long e = 896 + (r >> 56) % 256;
+        const unsigned long long low = (r >> 8) & 3;
+        bits = (r & 0x8000000000000000ull) | (e << 52) | (r & 0x000fffffe0000000ull) |
+               (low == 0 ? 0x10000000ull : low == 1 ? 0x0fffffffull : low == 2 ? 0x10000001ull : (r & 0x1fffffffull));
+        break;
+      }
+      case 2: {                 // the edges: around FLT_MIN and FLT_MAX, zeros
+        const unsigned long long e = ((r >> 60) & 1) ? 896 + 254 + ((r >> 56) & 3) : 894 + ((r >> 56) & 3);
+        bits = (r & 0x8000000000000000ull) | (e << 52) | (((r >> 61) & 1) ? 0x000fffffffffffffull : (r & 0x000fffffffffffffull));
+        if (((r >> 50) & 15) == 0) bits &= 0x8000000000000000ull;
+        break;
+      }
+      default: bits = 0; break;
+    }
+    if ((t & 3) != 3) {
+      const double x = __longlong_as_double((long long)bits);
+      if (__float_as_uint(rgpu::narrow_mirror(x)) != __float_as_uint(rgpu::mirror_of(x))) ++local;
+    } else {
+      const unsigned f = (unsigned)r;
+      const unsigned mag = f & 0x7fffffffu;
+      if (mag != 0 && mag < 0x00800000u) continue;  // FP32 subnormal
+      const float y = __uint_as_float(f);
+      const double a = rgpu::widen_f32(y), b = (double)y;
+      if (__double_as_longlong(a) != __double_as_longlong(b) && !(isnan(a) && isnan(b))) ++local;
+    }
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
+
+extern "C" int rhyme_gpu_check_conversions(long long n, unsigned long long seed, unsigned long long* mismatches) {
+  if (n < 0 || !mismatches) return RHYME_GPU_EINVAL;
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMalloc((void**)&d, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess && n > 0) {
+    conversion_check_kernel<<<1024, 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  return e == cudaSuccess ? RHYME_GPU_OK : RHYME_GPU_ECUDA;
+}
 
 extern "C" int rhyme_gpu_rate_probe(int kind, int iters, double* ops_per_second, double* ms) {
   if (kind < 0 || kind > 8 || iters < 1 || !ops_per_second) return RHYME_GPU_EINVAL;

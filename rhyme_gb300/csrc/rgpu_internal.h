@@ -179,6 +179,41 @@ __device__ __forceinline__ float mirror_of(double x) {
   return (fabsf(f) < FLT_MIN) ? copysignf(0.f, f) : f;
 }
 
+// FP32 <-> FP64 conversions of the state update by integer operations. The
+// FP64 pipe of GB300 converts at the rate of its FP64 adds, about 1/70 of
+// the FP32 rate; the last sweep converts each component twice per cell.
+// widen_f32: exact; FP32 zero and subnormal (never formed: -ftz) give a
+// zero of the same sign, inf and NaN go through the hardware conversion.
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned mag = b & 0x7fffffffu;
+  if (mag >= 0x7f800000u) return (double)f;
+  const unsigned sign = b & 0x80000000u;
+  const bool normal = mag >= 0x00800000u;
+  // exponent rebiased by 1023 - 127 = 896, mantissa moved up by 29 bits
+  const unsigned hi = normal ? (sign | ((mag >> 3) + 0x38000000u)) : sign;
+  const unsigned lo = normal ? (b << 29) : 0u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// narrow_mirror: mirror_of(x) (round to nearest even, subnormals flushed),
+// by integer operations where the result is a normal FP32 number, an
+// overflow to infinity, or x is zero; otherwise through mirror_of.
+__device__ __forceinline__ float narrow_mirror(double x) {
+  const unsigned long long t = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(t >> 32) & 0x80000000u;
+  const unsigned long long mag = t & 0x7fffffffffffffffull;
+  const int e = (int)(mag >> 52) - 896;  // the FP32 biased exponent
+  if (e >= 1 && e <= 254) {
+    const unsigned rem = (unsigned)(mag & 0x1fffffffull);       // the 29 bits rounded off
+    unsigned r = (unsigned)((mag >> 29) - (896ull << 23));     // FP32 exponent and mantissa
+    r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;  // ties to even; a carry
+    return __uint_as_float(sign | r);                                          // moves into the exponent
+  }
+  if (mag == 0) return __uint_as_float(sign);
+  return mirror_of(x);
+}
+
 // Signal speed |v| + cs of a cell's FP32 state (the mixed CFL's); bad is set
 // for a non-positive density or a non-finite speed, which the maximum skips.
 template <int D>

@@ -114,7 +114,7 @@ __device__ __forceinline__ double accumulate(float dtdx, float fl, float fr, flo
     acc[oc] = __fmaf_rn(dtdx, d, a_prev);
   } else {
     const float tot = (MODE == LAST) ? __fmaf_rn(dtdx, d, a_prev) : __fmul_rn(dtdx, d);
-    const double un = __dadd_rn(u_prev, (double)tot);
+    const double un = __dadd_rn(u_prev, widen_f32(tot));
     Unew[oc] = un;
     return un;
   }
@@ -372,15 +372,19 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     if (ga > NA || gb > NB) continue;
     const long long o = offset(ga, gb);
     if (PRE_ACC || PRE_U) cp_async_wait_all();  // this thread's copies (same items as phase 0)
-    float un[D + 2];
+    double ud[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
-      un[c] = mirror_of(accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
-                                      PRE_ACC ? pre_acc[c * S * P + it] : 0.f, PRE_U ? pre_u[c * S * P + it] : 0.0,
-                                      (long long)c * F + o, acc, Unew));
+      ud[c] = accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
+                               PRE_ACC ? pre_acc[c * S * P + it] : 0.f, PRE_U ? pre_u[c * S * P + it] : 0.0,
+                               (long long)c * F + o, acc, Unew);
     if (carrying) {
+      float un[D + 2];
 #pragma unroll
-      for (int c = 0; c < D + 2; ++c) carry.Uf_next[(long long)c * F + o] = un[c];
+      for (int c = 0; c < D + 2; ++c) {
+        un[c] = narrow_mirror(ud[c]);
+        carry.Uf_next[(long long)c * F + o] = un[c];
+      }
       const float v = speed_f32<D>(M, un, sbad);
       if (v > smax) smax = v;
     }

@@ -34,7 +34,7 @@ EXPORTS = ["rhyme_gpu_abi_version", "rhyme_gpu_create", "rhyme_gpu_destroy", "rh
            "rhyme_gpu_riemann_solve", "rhyme_gpu_irs_exec", "rhyme_gpu_slope_limiter",
            "rhyme_gpu_half_step", "rhyme_gpu_profile_steps", "rhyme_gpu_box_status",
            "rhyme_gpu_fallback_count", "rhyme_gpu_mh_solve_noalloc", "rhyme_gpu_set_box_params",
-           "rhyme_gpu_tma_launches", "rhyme_gpu_rate_probe",
+           "rhyme_gpu_tma_launches", "rhyme_gpu_rate_probe", "rhyme_gpu_check_conversions",
            "rhyme_gpu_batch_create", "rhyme_gpu_batch_run", "rhyme_gpu_batch_dt", "rhyme_gpu_batch_destroy",
            "rhyme_gpu_server_create", "rhyme_gpu_server_submit", "rhyme_gpu_server_tick",
            "rhyme_gpu_server_request", "rhyme_gpu_server_stats", "rhyme_gpu_server_last_error",
@@ -163,6 +163,7 @@ def load():
     L.rhyme_gpu_fallback_count.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     L.rhyme_gpu_tma_launches.argtypes = [C.POINTER(C.c_longlong)]
     L.rhyme_gpu_rate_probe.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.rhyme_gpu_check_conversions.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
     L.rhyme_gpu_sweep_plan.argtypes = [vp, C.c_int, dp, ip, ip]
     L.rhyme_gpu_output_level.argtypes = [vp, ip, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_longlong]
     L.rhyme_gpu_output_wait.argtypes = [vp]
@@ -594,6 +595,17 @@ def tma_launches():
 
 RATE_KINDS = ["fp64_fma_flops", "fp64_div", "fp64_sqrt", "fp64_pow", "fp32_fma_flops", "fp32_div_approx",
               "fp32_pow_exp2_log2", "fp64_add", "fp64_fp32_conversions"]
+
+
+def check_conversions(n, seed=0):
+    """Mismatches of the integer FP64 <-> FP32 conversions of the mixed state
+    update against the hardware conversions over n values
+    (rhyme_gpu_check_conversions)."""
+    bad = C.c_ulonglong()
+    rc = load().rhyme_gpu_check_conversions(int(n), int(seed), C.byref(bad))
+    if rc != OK:
+        raise RhymeGpuError(rc, "rhyme_gpu_check_conversions")
+    return bad.value
 
 
 def rate_probe(kind, iters=2000):
