@@ -82,21 +82,28 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),
+// acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
+enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
+
 // Threads of a tile's CTA: one per interface of the tile ((S+1)·P, the
 // costliest phase), rounded up to whole warps, so that no phase but the
 // shared-memory staging needs a second, mostly idle round behind a barrier;
-// at most 512. CTAs per SM such that a thread may keep up to 56 registers
-// (4 CTAs of 288 threads: the sweeps use 50-52 without spilling).
+// at most 512. CTAs per SM (ctas<MODE>) such that a thread may keep up to
+// 44 registers in the sweeps that only accumulate (5 CTAs of 288 threads;
+// measured 4 % faster than 4 CTAs at 56) and 56 in the sweeps that form
+// U^{n+1} (4 CTAs: at 44 registers these spill and lose 10 %).
 template <int S, int P>
 struct TileCfg {
   static constexpr int warps_ = ((S + 1) * P + 31) / 32;
   static constexpr int threads = warps_ * 32 > 512 ? 512 : warps_ * 32;
-  static constexpr int min_ctas = 65536 / (threads * 56) > 0 ? 65536 / (threads * 56) : 1;
+  template <int MODE>
+  static constexpr int ctas() {
+    constexpr int regs = (MODE == LAST || MODE == ONLY) ? 56 : 44;
+    return 65536 / (threads * regs) > 0 ? 65536 / (threads * regs) : 1;
+  }
 };
 
-// Sweep modes: the flux difference X of this axis becomes acc = X (FIRST),
-// acc += X (MID), U^{n+1} = U + (acc + X) (LAST) or U^{n+1} = U + X (ONLY).
-enum { FIRST = 0, MID = 1, LAST = 2, ONLY = 3 };
 
 // The flux difference dt/dx (F_left - F_right) of one component of one cell
 // and its accumulation by mode, with explicit roundings (a fused
@@ -393,7 +400,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
 }
 
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
+__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::template ctas<MODE>())
     sweep_kernel(MixedParams M, const float* __restrict__ Uf, const double* __restrict__ U, Geom g,
                  Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
                  double* __restrict__ Unew, FallbackQueue q, const __grid_constant__ CUtensorMap map,
@@ -415,7 +422,7 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_cta
 // The same sweep over the tiles of a batch of boxes, taken from a work queue
 // (item.chunk = the tile's linear index tA + nA * (tB + nB * (cC - 1))).
 template <int D, int A, int S, int P, int MODE>
-__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::min_ctas)
+__global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::template ctas<MODE>())
     batch_sweep_kernel(MixedParams M, const BoxDesc* __restrict__ TB, const WorkItem* __restrict__ items,
                        int n, int* head, FallbackQueue q) {
   constexpr int B = Axes<D, A>::B;

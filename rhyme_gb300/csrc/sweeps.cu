@@ -69,7 +69,9 @@ template <int D, int A, int S, int P>
 cudaError_t launch_batch_one(const MixedParams& M, const BoxDesc* TB, const WorkItem* items, int n, int* head,
                              const FallbackQueue& q, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  batch_sweep_kernel<D, A, S, P, mode_of<D, A>()><<<152 * TileCfg<S, P>::min_ctas, TileCfg<S, P>::threads, 0, st>>>(M, TB, items, n, head, q);
+  constexpr int MODE = mode_of<D, A>();
+  batch_sweep_kernel<D, A, S, P, MODE><<<152 * TileCfg<S, P>::template ctas<MODE>(), TileCfg<S, P>::threads, 0, st>>>(
+      M, TB, items, n, head, q);
   return cudaGetLastError();
 }
 
