@@ -127,7 +127,8 @@ __global__ void conversion_check_kernel(long long n, unsigned long long seed, un
     }
     if ((t & 3) != 3) {
       const double x = __longlong_as_double((long long)bits);
-      if (__float_as_uint(rgpu::narrow_mirror(x)) != __float_as_uint(rgpu::mirror_of(x))) ++local;
+      const float a = rgpu::narrow_mirror(x), b = rgpu::mirror_of(x);
+      if (__float_as_uint(a) != __float_as_uint(b) && !(isnan(a) && isnan(b))) ++local;
     } else {
       const unsigned f = (unsigned)r;
       const unsigned mag = f & 0x7fffffffu;

@@ -104,6 +104,7 @@ extern "C" int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params, const 
   d.min = d.v[0];
   for (int a = 1; a < D; ++a)
     if (d.v[a] < d.min) d.min = d.v[a];
+  for (int a = 0; a < 3; ++a) d.inv_f[a] = (float)(1.0 / d.v[a]);
 
   StepScratch s;
   s.dt = base;

@@ -134,7 +134,8 @@ struct StepScratch {
 
 struct Dx {
   double v[3];
-  double min;  // minval(dx(1:NDIM))
+  double min;    // minval(dx(1:NDIM))
+  float inv_f[3];  // 1/dx in FP32 (the mixed sweeps' dt/dx = FP32(dt) * inv_f)
 };
 
 }  // namespace rgpu
@@ -182,36 +183,50 @@ __device__ __forceinline__ float mirror_of(double x) {
 // FP32 <-> FP64 conversions of the state update by integer operations. The
 // FP64 pipe of GB300 converts at the rate of its FP64 adds, about 1/70 of
 // the FP32 rate; the last sweep converts each component twice per cell.
-// widen_f32: exact; FP32 zero and subnormal (never formed: -ftz) give a
-// zero of the same sign, inf and NaN go through the hardware conversion.
+// widen_f32: exact; an FP32 zero or subnormal (never formed: -ftz) gives a
+// zero of the same sign, an infinity an infinity, a NaN a quiet NaN with the
+// payload moved up. No path through the FP64 pipe.
 __device__ __forceinline__ double widen_f32(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned mag = b & 0x7fffffffu;
-  if (mag >= 0x7f800000u) return (double)f;
   const unsigned sign = b & 0x80000000u;
-  const bool normal = mag >= 0x00800000u;
-  // exponent rebiased by 1023 - 127 = 896, mantissa moved up by 29 bits
-  const unsigned hi = normal ? (sign | ((mag >> 3) + 0x38000000u)) : sign;
-  const unsigned lo = normal ? (b << 29) : 0u;
+  unsigned hi, lo;
+  if (mag >= 0x7f800000u) {  // infinity, NaN
+    hi = sign | 0x7ff00000u | ((mag & 0x007fffffu) >> 3) | (mag != 0x7f800000u ? 0x00080000u : 0u);
+    lo = b << 29;
+  } else if (mag >= 0x00800000u) {  // normal: exponent rebiased by 1023 - 127 = 896
+    hi = sign | ((mag >> 3) + 0x38000000u);
+    lo = b << 29;
+  } else {
+    hi = sign;
+    lo = 0u;
+  }
   return __hiloint2double((int)hi, (int)lo);
 }
 
-// narrow_mirror: mirror_of(x) (round to nearest even, subnormals flushed),
-// by integer operations where the result is a normal FP32 number, an
-// overflow to infinity, or x is zero; otherwise through mirror_of.
+// narrow_mirror: mirror_of(x) (round to nearest even, an FP32 subnormal
+// flushed to a zero of the same sign) by integer operations only; an
+// overflow gives an infinity, a NaN a quiet NaN.
 __device__ __forceinline__ float narrow_mirror(double x) {
   const unsigned long long t = (unsigned long long)__double_as_longlong(x);
   const unsigned sign = (unsigned)(t >> 32) & 0x80000000u;
   const unsigned long long mag = t & 0x7fffffffffffffffull;
   const int e = (int)(mag >> 52) - 896;  // the FP32 biased exponent
+  unsigned r;
   if (e >= 1 && e <= 254) {
-    const unsigned rem = (unsigned)(mag & 0x1fffffffull);       // the 29 bits rounded off
-    unsigned r = (unsigned)((mag >> 29) - (896ull << 23));     // FP32 exponent and mantissa
+    const unsigned rem = (unsigned)(mag & 0x1fffffffull);  // the 29 bits rounded off
+    r = (unsigned)((mag >> 29) - (896ull << 23));         // FP32 exponent and mantissa
     r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;  // ties to even; a carry
-    return __uint_as_float(sign | r);                                          // moves into the exponent
+  } else if (e <= 0) {                                                       // moves into the exponent
+    // below FLT_MIN: flushed, unless it rounds up to FLT_MIN
+    // (x >= 2^-126 (1 - 2^-24), ties included)
+    r = (e == 0 && (mag & 0x000fffffffffffffull) >= 0x000fffffe0000000ull) ? 0x00800000u : 0u;
+  } else if (mag > 0x7ff0000000000000ull) {  // NaN
+    r = 0x7fc00000u | (unsigned)((mag & 0x000fffffffffffffull) >> 29);
+  } else {  // overflow, infinity
+    r = 0x7f800000u;
   }
-  if (mag == 0) return __uint_as_float(sign);
-  return mirror_of(x);
+  return __uint_as_float(sign | r);
 }
 
 // Signal speed |v| + cs of a cell's FP32 state (the mixed CFL's); bad is set

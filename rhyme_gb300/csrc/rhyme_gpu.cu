@@ -284,6 +284,7 @@ Dx make_dx(int D, const double dx[3]) {
   d.min = d.v[0];
   for (int a = 1; a < D; ++a)
     if (d.v[a] < d.min) d.min = d.v[a];
+  for (int a = 0; a < 3; ++a) d.inv_f[a] = (float)(1.0 / d.v[a]);
   return d;
 }
 

@@ -200,8 +200,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
   const int a0 = tA * S + 1;  // first interior cell of the slab along A
   const int b0 = tB * P + 1;
   const long long F = g.field;
-  // dt/dx and (0.5 dt)/dx once per CTA (FP64 divisions are scarce on
-  // GB300), formed by a thread outside the warp that issues and polls the
+  // dt/dx and (0.5 dt)/dx once per CTA in FP32 (FP32(dt) times the FP32
+  // inverse of dx: an FP64 division per CTA kept the FP64 pipe about 9 %
+  // busy), formed by a thread outside the warp that issues and polls the
   // staging copy, while the copy is in flight
   __shared__ float s_dtdx[2];
   constexpr int kDtThread = TileCfg<S, P>::threads > 32 ? 32 : 0;
@@ -261,9 +262,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
       tma_load_4d(su, tma.map, co[0], co[1], co[2], 0, bar, (unsigned)((D + 2) * PLANE * sizeof(float)));
     }
     if (threadIdx.x == kDtThread) {
-      const double dt = *dtp;
-      s_dtdx[0] = (float)(dt / dx.v[A]);
-      s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+      const float dt = __double2float_rn(*dtp);
+      s_dtdx[0] = dt * dx.inv_f[A];
+      s_dtdx[1] = (0.5f * dt) * dx.inv_f[A];
     }
     // one warp polls the barrier; the others wait at the CTA barrier below,
     // off the issue slots the co-resident CTAs are computing with
@@ -274,9 +275,9 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     parity ^= 1u;
   } else {
     if (threadIdx.x == kDtThread) {
-      const double dt = *dtp;
-      s_dtdx[0] = (float)(dt / dx.v[A]);
-      s_dtdx[1] = (float)(0.5 * dt / dx.v[A]);
+      const float dt = __double2float_rn(*dtp);
+      s_dtdx[0] = dt * dx.inv_f[A];
+      s_dtdx[1] = (0.5f * dt) * dx.inv_f[A];
     }
     for (int it = threadIdx.x; it < (S + 4) * P; it += TileCfg<S, P>::threads) {
       int la, lb;
