@@ -98,15 +98,30 @@ __device__ __forceinline__ T sp_int_e(const T* u) {
   return u[D + 1] / u[0] - sp_kin_e<D>(u);
 }
 
+// The FP32 forms of the mixed sweeps (pressure, sound speed, flux) are the
+// same quantities with fewer divisions: p = (E - |m|^2 / (2 rho)) (gamma-1)
+// for rho e_int (gamma-1), cs = sqrt(gamma p / rho) for
+// sqrt(gamma kB/amu T/mu), and the flux from one reciprocal of rho. FP32
+// division is a reciprocal and a multiply plus range handling; the sweeps
+// divide a lot (256^3 mixed step 2.43 -> 2.20 ms, L1(rho) against FP64 a
+// little lower). The double forms keep the reference's operations.
+
 // rhyme_ideal_gas_pressure.f90:9
 template <int D, typename T>
 __device__ __forceinline__ T pressure(const Gas<T>& G, const T* u) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    T s = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) s = s + u[1 + a] * u[1 + a];
+    return (u[D + 1] - T(0.5) * s / u[0]) * G.gm1;
+  }
   return u[0] * sp_int_e<D>(u) * G.gm1;
 }
 
 // rhyme_ideal_gas_temperature_per_mu.f90:9-10, _speed_of_sound.f90:9
 template <int D, typename T>
 __device__ __forceinline__ T sound_speed(const Gas<T>& G, const T* u) {
+  if constexpr (sizeof(T) == sizeof(float)) return m_sqrt(G.g * pressure<D>(G, u) / u[0]);
   T t_mu = sp_int_e<D>(u) * G.gm1 / G.kb_amu;
   return m_sqrt(G.g_kb_amu * t_mu);
 }
@@ -117,6 +132,20 @@ __device__ __forceinline__ void flux(const Gas<T>& G, const T* u, T* f) {
   if (m_abs(u[0]) < Limits<T>::tiny()) {
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) f[c] = T(0);
+    return;
+  }
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const T inv = T(1) / u[0];
+    T s = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) s = s + u[1 + a] * u[1 + a];
+    const T p = (u[D + 1] - T(0.5) * s * inv) * G.gm1;
+    const T vn = u[1 + AX] * inv;
+    f[0] = u[1 + AX];
+#pragma unroll
+    for (int a = 0; a < D; ++a) f[1 + a] = u[1 + a] * vn;
+    f[1 + AX] = f[1 + AX] + p;
+    f[D + 1] = vn * (u[D + 1] + p);
     return;
   }
   T p = pressure<D>(G, u);
@@ -661,6 +690,172 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       rp_sampling<D, AX>(G, L, R, l, r, s, dxdt, u);
     }
   }
+}
+
+// ---- the mixed form's FP32 interface flux ----------------------------------
+// rhyme_riemann_problem_solve.f90:17-103 sampled at x/t = 0 (every interface
+// of the sweeps) followed by rhyme_ideal_gas_flux.f90, in FP32, for the
+// interfaces the FP64 solver need not redo: a density at or below the
+// vacuum density on either side (every vacuum branch), vacuum generation or
+// an interface within 10 % of it, a density or pressure ratio beyond 1e6,
+// and a first guess whose Newton iteration misses the tolerance set *need64
+// instead, and the caller queues the interface for rp_solve<double>. The
+// algorithm is the FP64 one's: the adaptive first guess of
+// rhyme_irs_guess_p_star.f90:14-38, the Newton iteration of
+// rhyme_irs_exec.f90:28-39 on the wave functions of
+// rhyme_irs_nonlinear_wave_function.f90, the sampled side's star state
+// (rhyme_riemann_problem_star.f90:40-65) and the tests of
+// rhyme_riemann_problem_sampling.f90:13-47 at x/t = 0, including the fan of
+// rhyme_riemann_problem_w_kfan.f90. The FP32 arithmetic is arranged for
+// fewer divisions (one reciprocal per side of rho, p and rho cs; the
+// quotients of gamma from Gas; the convergence test multiplied out; the flux
+// formed from the sampled primitive state instead of from its conserved
+// form), which also skips the cancellation of E - |m|^2/(2 rho).
+__device__ __forceinline__ void wave_f32(const Gas<float>& G, float Ak, float Bk, float c2g, float irc, float pk,
+                                         float ipk, float p, float& f, float& fprime) {
+  if (p > pk) {
+    const float rb = 1.f / (Bk + p);
+    const float factor = sqrtf(Ak * rb);
+    f = (p - pk) * factor;
+    fprime = factor * (1.f - 0.5f * (p - pk) * rb);
+  } else {
+    // (p/p_k)^e - 1 as expm1(e log1p((p - p_k)/p_k)) (see nonlinear_wave)
+    const float t = log1pf((p - pk) * ipk);
+    f = c2g * expm1f(G.gm1_2g * t);
+    fprime = irc * expf(-G.gp1_2g * t);
+  }
+}
+
+template <int D, int AX>
+__device__ __forceinline__ void rp_flux_f32(const Gas<float>& G, const Rp<float>& rp, const float* l,
+                                            const float* r, float* f, bool* need64) {
+  const float e_rho = rp.vac_rho_next;
+  if (!(fmax_ref(l[0], rp.vac_rho) >= e_rho) || !(fmax_ref(r[0], rp.vac_rho) >= e_rho)) {
+    *need64 = true;
+    return;
+  }
+  // both densities above the vacuum density: the clamp of rho is inactive
+  const float rl = l[0], rr = r[0];
+  const float il = 1.f / rl, ir = 1.f / rr;
+  float sl = 0.f, sr = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    sl = sl + l[1 + a] * l[1 + a];
+    sr = sr + r[1 + a] * r[1 + a];
+  }
+  const float pl_raw = (l[D + 1] - 0.5f * sl * il) * G.gm1;
+  const float pr_raw = (r[D + 1] - 0.5f * sr * ir) * G.gm1;
+  const float pl = fmax_ref(pl_raw, rp.vac_p), pr = fmax_ref(pr_raw, rp.vac_p);
+  const float cl = fmax_ref(sqrtf(G.g * pl_raw * il), FLT_MIN);
+  const float cr = fmax_ref(sqrtf(G.g * pr_raw * ir), FLT_MIN);
+  const float vl = l[1 + AX] * il, vr = r[1 + AX] * ir;
+  const float du = vr - vl;
+  const float du_crit = G.two_gm1 * (cl + cr);
+  const float rmin = fmin_ref(rl, rr), rmax = fmax_ref(rl, rr);
+  const float pmin = fmin_ref(pl, pr), pmax = fmax_ref(pl, pr);
+  if (!(du_crit - du > 0.1f * du_crit) || !(rmin * 1e6f > rmax) || !(pmin * 1e6f > pmax)) {
+    *need64 = true;
+    return;
+  }
+  const float ipl = 1.f / pl, ipr = 1.f / pr;
+  const float ircl = il / cl, ircr = ir / cr;  // 1/(rho cs)
+  // the adaptive first guess
+  float p;
+  {
+    const float cup = 0.25f * (rl + rr) * (cl + cr);
+    const float ppv = fmax_ref(0.5f * (pl + pr) + 0.5f * (vl - vr) * cup, 0.f);
+    if (pmax <= 2.f * pmin && (pmin < ppv && ppv < pmax)) {
+      p = ppv;  // PVRS
+    } else if (ppv < pmin) {  // two-rarefaction
+      const float icl = ircl * rl, icr = ircr * rr;  // 1/cs
+      const float pq = m_pow(pl * ipr, G.gm1_2g);
+      const float um = (pq * vl * icl + vr * icr + G.two_gm1 * (pq - 1.f)) / (pq * icl + icr);
+      const float ptl = 1.f + G.half_gm1 * (vl - um) * icl;
+      const float ptr = 1.f + G.half_gm1 * (um - vr) * icr;
+      p = 0.5f * (pl * m_pow(ptl, G.inv_gm1_2g) + pr * m_pow(ptr, G.inv_gm1_2g));
+    } else {  // two-shock
+      const float gel = sqrtf(G.two_gp1 * il / (G.gm1_gp1 * pl + ppv));
+      const float ger = sqrtf(G.two_gp1 * ir / (G.gm1_gp1 * pr + ppv));
+      p = (gel * pl + ger * pr - du) / (gel + ger);
+    }
+    p = fmax_ref(p, FLT_MIN);
+  }
+  // Newton iteration from it
+  const float Akl = G.two_gp1 * il, Bkl = G.gm1_gp1 * pl, c2gl = G.two_gm1 * cl;
+  const float Akr = G.two_gp1 * ir, Bkr = G.gm1_gp1 * pr, c2gr = G.two_gm1 * cr;
+  float p_prev = p, fl = 0.f, fr = 0.f, fpl, fpr;
+  bool conv = false;
+  for (int i = 1; i <= rp.n_iter; ++i) {
+    wave_f32(G, Akl, Bkl, c2gl, ircl, pl, ipl, p, fl, fpl);
+    wave_f32(G, Akr, Bkr, c2gr, ircr, pr, ipr, p, fr, fpr);
+    p = p_prev - (fl + fr + du) / (fpl + fpr);
+    if (p < 0.f) break;
+    if (2.f * fabsf(p - p_prev) < rp.tol * (p + p_prev)) {
+      conv = true;
+      break;
+    }
+    p_prev = p;
+  }
+  if (!conv) {
+    *need64 = true;
+    return;
+  }
+  const float ps = (p < rp.vac_p) ? rp.vac_p : p;
+  const float us = 0.5f * ((vr + vl) + (fr - fl));
+  // the sampled side at x/t = 0: its density, normal velocity and pressure
+  float rho, vn, pp;
+  const bool right = 0.f > us;
+  bool fan = false;
+  float fan_cs = 0.f, fan_ic = 0.f, fan_v = 0.f, fan_rho = 0.f, fan_p = 0.f;
+  if (right) {  // right of the contact
+    const float ps_pr = ps * ipr;
+    if (ps > pr) {
+      const float rs = rr * (G.gm1_gp1 + ps_pr) / (G.gm1_gp1 * ps_pr + 1.f);
+      const float speed = vr + cr * sqrtf(G.gp1_2g * ps_pr + G.gm1_2g);
+      if (0.f < speed) { rho = rs; vn = us; pp = ps; } else { rho = rr; vn = vr; pp = pr; }
+    } else {
+      float pg, pa;
+      m_pow2(ps_pr, G.g_inv, G.gm1_2g, pg, pa);
+      if (0.f < us + cr * pa) { rho = rr * pg; vn = us; pp = ps; }
+      else if (0.f < vr + cr) { fan = true; fan_cs = -cr; fan_ic = -(ircr * rr); fan_v = vr; fan_rho = rr; fan_p = pr; }
+      else { rho = rr; vn = vr; pp = pr; }
+    }
+  } else {  // left of the contact
+    const float ps_pl = ps * ipl;
+    if (ps > pl) {
+      const float rs = rl * (G.gm1_gp1 + ps_pl) / (G.gm1_gp1 * ps_pl + 1.f);
+      const float speed = vl - cl * sqrtf(G.gp1_2g * ps_pl + G.gm1_2g);
+      if (0.f > speed) { rho = rs; vn = us; pp = ps; } else { rho = rl; vn = vl; pp = pl; }
+    } else {
+      float pg, pa;
+      m_pow2(ps_pl, G.g_inv, G.gm1_2g, pg, pa);
+      if (0.f > us - cl * pa) { rho = rl * pg; vn = us; pp = ps; }
+      else if (0.f > vl - cl) { fan = true; fan_cs = cl; fan_ic = ircl * rl; fan_v = vl; fan_rho = rl; fan_p = pl; }
+      else { rho = rl; vn = vl; pp = pl; }
+    }
+  }
+  if (fan) {  // inside the rarefaction fan (w_kfan at x/t = 0)
+    const float base = G.two_gp1 + G.gm1_gp1 * fan_ic * fan_v;
+    float prho, ppw;
+    m_pow2(base, G.two_gm1, G.inv_gm1_2g, prho, ppw);
+    rho = fan_rho * prho;
+    vn = G.two_gp1 * (fan_cs + G.half_gm1 * fan_v);
+    pp = fan_p * ppw;
+  }
+  // the flux of the sampled primitive state
+  float v[D];
+  float s = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    v[a] = (a == AX) ? vn : (right ? r[1 + a] * ir : l[1 + a] * il);
+    s = s + v[a] * v[a];
+  }
+  const float mn = rho * vn;
+  f[0] = mn;
+#pragma unroll
+  for (int a = 0; a < D; ++a) f[1 + a] = mn * v[a];
+  f[1 + AX] = f[1 + AX] + pp;
+  f[D + 1] = vn * (0.5f * rho * s + pp * (0.5f * G.two_gm1) + pp);
 }
 
 // Interface flux: Riemann state at x/t = 0 (dx = 0 in

@@ -100,6 +100,7 @@ extern "C" int rhyme_gpu_mh_solve_noalloc(const rhyme_gpu_params* params, const 
   make_dev_params(params, &P);
 
   Dx d;
+  memset(&d, 0, sizeof d);
   for (int a = 0; a < 3; ++a) d.v[a] = (a < D) ? dx[a] : 1.0;
   d.min = d.v[0];
   for (int a = 1; a < D; ++a)

@@ -279,6 +279,7 @@ void destroy_box(Box* b, cudaStream_t st) {
 
 Dx make_dx(int D, const double dx[3]) {
   Dx d;
+  memset(&d, 0, sizeof d);  // padding too: steps compare Dx values bytewise
   for (int a = 0; a < 3; ++a) d.v[a] = (a < D) ? dx[a] : 1.0;
   // minval(samr%levels(0)%dx), rhyme_cfl_time_step.f90:74
   d.min = d.v[0];

@@ -319,16 +319,15 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     int li, lb;
     split(it, S + 1, li, lb);
     if (a0 - 1 + li > NA || b0 + lb > NB) continue;
-    float l[D + 2], r[D + 2], u[D + 2], f[D + 2];
+    float l[D + 2], r[D + 2], f[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c) {
       l[c] = sh.ur[c][ix(li, lb, S + 2)];
       r[c] = sh.ul[c][ix(li + 1, lb, S + 2)];
     }
     bool need64 = false;
-    rp_solve<D, A, float, true>(M.G, M.rp, l, r, 0.f, u, &need64);
+    rp_flux_f32<D, A>(M.G, M.rp, l, r, f, &need64);
     if (!need64) {
-      flux<D, A>(M.G, u, f);
 #pragma unroll
       for (int c = 0; c < D + 2; ++c)
         if (!isfinite(f[c])) need64 = true;
