@@ -244,13 +244,15 @@ def allsum(x, world):
     return reduce_scalar(x, world, "sum", device="cuda")
 
 
-def launches_per_step(prec, ndim):
+def launches_per_step(prec, ndim, fused_xy=False):
     """Kernels of this library launched per single-box step: FP64 cfl, ghost
-    fill, faces, fluxes, update; mixed cfl (which also writes the FP32
-    mirror), ghost fill (of the FP64 state and of the mirror, in one
-    kernel), one sweep per axis and the FP64 fix-up of the queued
-    interfaces."""
-    return 5 if prec == "fp64" else 3 + ndim
+    fill, faces, fluxes, update; mixed cfl (carried, or the whole pass that
+    also writes the FP32 mirror), ghost fill (of the FP64 state and of the
+    mirror, in one kernel), one sweep per axis (one kernel for x and y of a
+    3-D box where fused_xy) and the FP64 fix-up of the queued interfaces."""
+    if prec == "fp64":
+        return 5
+    return 3 + ndim - (1 if fused_xy else 0)
 
 
 def advance_steps(args, cfg):
@@ -516,9 +518,11 @@ def run_gpu(args, rank, local, world):
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": traffic, "bytes_per_cell_update": bpc,
                              "step_achieved": value / world * bpc / 1e9,
-                             "note": "compute-bound: FP64 pipe (plain) / FP32 pipe and SFU (mixed), not HBM"},
+                             "note": "compute-bound: FP64 pipe (plain) / FP32 issue (mixed), not HBM; the "
+                                     "step's 80 B per cell charged to its longest kernel" +
+                                     (", which runs the x and y sweeps of the step" if dom == "sweep_xy" else "")},
                 "phases_ms": phases, "clocks": clk,
-                "gpu_launches": launches_per_step(prec, ndim) * K,
+                "gpu_launches": launches_per_step(prec, ndim, "sweep_xy" in phases) * K,
                 "cpu_baseline": cpu}
         if cmp is not None:
             line["vs_fp64"] = cmp

@@ -235,8 +235,10 @@ int rhyme_gpu_run(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
  * context stream; ms[5] receives the mean milliseconds per launch of the
  * phases cfl, ghost_fill, faces, fluxes, update (RHYME_GPU_FP64) or cfl,
  * ghost_fill, sweep_x, sweep_y, sweep_z (RHYME_GPU_MIXED; the last one that
- * runs includes the FP64 fix-up, absent axes read 0). The state advances
- * nsteps steps exactly as rhyme_gpu_run would advance it.
+ * runs includes the FP64 fix-up, absent axes read 0; in a 3-D box whose x
+ * and y sweeps ran as one kernel, ms[2] is that kernel and ms[3] is -1).
+ * The state advances nsteps steps exactly as rhyme_gpu_run would advance
+ * it.
  */
 int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const double dx[3],
                             int nsteps, double ms[5]);

@@ -528,14 +528,30 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
                                   double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev,
-                                  const SweepCarry& carry) {
+                                  const SweepCarry& carry, int* fused) {
   // ev (optional, 3 events): recorded after the x sweep, after the y sweep
   // and at the end (the z sweep and the FP64 fix-up); absent axes record
-  // at the same point.
+  // at the same point, and so do both when one kernel ran the x and y
+  // sweeps (*fused, optional, is then 1).
   const int D = M.ndim;
   if (D < 1 || D > 3) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(q.n, 0, sizeof(int), st);
-  for (int a = 0; a < D; ++a) {
+  int first = 0;
+  if (fused) *fused = 0;
+  if (e == cudaSuccess && D == 3 && plan.fuse_xy) {
+    // the x and y sweeps in one kernel where the mirror's rows allow the
+    // plane's tensor copy (bit-identical to the two sweeps)
+    e = launch_sweep_xy_3(M, Uf, g, dx, s.dt, acc, q, st);
+    if (e == cudaSuccess) {
+      first = 2;
+      if (fused) *fused = 1;
+      if (ev) e = cudaEventRecord(ev[0], st);
+      if (e == cudaSuccess && ev) e = cudaEventRecord(ev[1], st);
+    } else if (e == cudaErrorNotSupported) {
+      e = cudaSuccess;
+    }
+  }
+  for (int a = first; a < D; ++a) {
     if (e == cudaSuccess)
       e = launch_sweep_axis(D, a, plan.shape[a], M, Uf, U, g, dx, s.dt, acc, Unew, q, st,
                             a == D - 1 ? carry : SweepCarry());
@@ -687,6 +703,27 @@ bool encode_mirror_map(CUtensorMap* out, const float* Uf, const Geom& g, int D, 
   } else {
     box[0] = (cuuint32_t)(P + 4);
   }
+  for (int i = 0; i < 4; ++i)
+    if (box[i] > 256 || box[i] > dim[i]) return false;
+  if ((box[0] * 4) % 16 != 0) return false;
+  cuuint32_t estride[4] = {1, 1, 1, 1};
+  const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)Uf, dim, stride, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  g_tma_launches.fetch_add(1, std::memory_order_relaxed);
+  return true;
+}
+
+bool encode_xy_map(CUtensorMap* out, const float* Uf, const Geom& g, int TX, int TY) {
+  const EncodeTiledFn fn = encoder();
+  if (!fn) return false;
+  const long long X = g.s[1], Y = g.s[2] / g.s[1], Z = g.field / g.s[2];
+  if (X % 4 != 0 || ((uintptr_t)Uf % 16) != 0) return false;
+  cuuint64_t dim[4] = {(cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, 5};
+  cuuint64_t stride[3] = {(cuuint64_t)X * 4, (cuuint64_t)(X * Y) * 4, (cuuint64_t)g.field * 4};
+  // one z plane of the tile with its 2-cell halo along x and y, every component
+  cuuint32_t box[4] = {(cuuint32_t)(TX + 4), (cuuint32_t)(TY + 4), 1, 5};
   for (int i = 0; i < 4; ++i)
     if (box[i] > 256 || box[i] > dim[i]) return false;
   if ((box[0] * 4) % 16 != 0) return false;

@@ -88,6 +88,7 @@ inline int default_sweep_shape(int ndim, int axis, int nA) {
 // Tile shape per axis of one box's mixed sweeps.
 struct SweepPlan {
   int shape[3];
+  int fuse_xy = 0;  // 3-D: the x and y sweeps as one kernel (sweep_xy_kernel) where it can run
 };
 
 // Geometry of one box in the reference layout: component blocks of
@@ -269,7 +270,15 @@ cudaError_t launch_mh_solve_mixed(const MixedParams& M, const double* U, const f
                                   double* Unew, float* acc, const Geom& g,
                                   const Dx& dx, const StepScratch& s, const FallbackQueue& q,
                                   const SweepPlan& plan, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                                  const SweepCarry& carry = SweepCarry());
+                                  const SweepCarry& carry = SweepCarry(), int* fused = nullptr);
+// The x and y sweeps of a 3-D box as one kernel (sweeps.cu, sweep_xy_kernel):
+// cudaErrorNotSupported where its tensor copy cannot be used (rows of the
+// mirror not a multiple of 16 bytes, the encoder unavailable, too many tiles);
+// the caller then runs the two sweeps.
+cudaError_t launch_sweep_xy_3(const MixedParams& M, const float* Uf, const Geom& g, const Dx& dx,
+                              const double* dtp, float* acc, const FallbackQueue& q, cudaStream_t st);
+// The tensor map of sweep_xy_kernel's plane copies (kernels_mixed.cu).
+bool encode_xy_map(CUtensorMap* out, const float* Uf, const Geom& g, int TX, int TY);
 cudaError_t launch_ghost_fill_f32(const DevParams& P, float* Uf, const Geom& g, cudaStream_t st);
 // The mixed solve of the slab of interior cells [lo, hi] of the outermost
 // axis: its sweeps, then the FP64 fix-up of the queue entries from *done on,

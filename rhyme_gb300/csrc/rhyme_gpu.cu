@@ -90,6 +90,7 @@ struct rhyme_gpu_ctx {
   DevParams dp{};
   MixedParams mp{};
   bool mixed = false;
+  bool fuse_xy = true;  // 3-D mixed: the x and y sweeps as one kernel (RHYME_GPU_XY=0: two)
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
@@ -309,6 +310,8 @@ int rhyme_gpu_create(rhyme_gpu_ctx** out, const rhyme_gpu_params* params) {
   make_dev_params(params, &ctx->dp);
   make_mixed_params(ctx->dp, &ctx->mp);
   ctx->mixed = (params->precision == RHYME_GPU_MIXED);
+  const char* xy = getenv("RHYME_GPU_XY");
+  if (xy && atoi(xy) == 0) ctx->fuse_xy = false;
   const char* to = getenv("RHYME_GPU_TIMEOUT_S");
   if (to && atof(to) > 0) ctx->timeout_s = atof(to);
   cudaError_t e = cudaGetDevice(&ctx->device);
@@ -769,6 +772,7 @@ int box_plan(rhyme_gpu_ctx* ctx, Box* b, const Dx& dx) {
       b->plan.shape[a] = it->second;
     }
   }
+  b->plan.fuse_xy = (D == 3 && ctx->fuse_xy) ? 1 : 0;
   b->plan_valid = true;
   return RHYME_GPU_OK;
 }
@@ -1122,6 +1126,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
   double acc[5] = {0, 0, 0, 0, 0};
   int rc = RHYME_GPU_OK;
+  int fused = 0;
   for (int s = 0; s < nsteps && rc == RHYME_GPU_OK; ++s) {
     StepScratch sc = scratch_of(b, false);
     double* U = b->state[b->cur];
@@ -1138,7 +1143,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], ctx->stream);
       if (e == cudaSuccess)
         e = launch_mh_solve_mixed(b->mp, U, b->Uf[b->cur], V, b->acc, b->g, d, sc,
-                                  b->fbq, b->plan, ctx->stream, ev + 3, carry_of(b, b->cur));
+                                  b->fbq, b->plan, ctx->stream, ev + 3, carry_of(b, b->cur), &fused);
     } else {
       if (e == cudaSuccess) e = launch_cfl(b->dp, U, b->g, d, sc, ctx->stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
@@ -1160,6 +1165,7 @@ extern "C" int rhyme_gpu_profile_steps(rhyme_gpu_ctx* ctx, int handle, const dou
   }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 5; ++k) ms[k] = acc[k] / nsteps;
+  if (fused) ms[3] = -1.0;  // ms[2]: the x and y sweeps as one kernel
   b->carry_valid = ctx->mixed && rc == RHYME_GPU_OK;
   return rc;
 }

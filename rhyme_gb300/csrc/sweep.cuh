@@ -450,5 +450,196 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::templat
 }
 
 
+// ---- the x and y sweeps of a 3-D box in one kernel ---------------------------
+// A CTA takes a TX x TY tile of one z plane: one TMA copy stages the tile's
+// FP32 state with a 2-cell halo along x and y ((TX+4) x (TY+4) cells, every
+// component), then the x sweep (face states, FP32 interface fluxes, flux
+// differences held in registers) and the y sweep run on it, and the
+// accumulator acc = dt/dx X + dt/dy Y is written once. Every operation is
+// the per-axis sweeps' (FIRST then MID, the same explicit roundings), so
+// the result is bit-identical to sweep_kernel<3,0,...> followed by
+// sweep_kernel<3,1,...>; what it saves is the second staging of the slab
+// and the accumulator's round trip between the two sweeps (40 of the
+// step's 240 bytes per cell). One thread per x interface ((TX+1) TY,
+// rounded up to warps).
+template <int TX, int TY>
+struct XYCfg {
+  static constexpr int threads = (((TX + 2) * TY > (TX + 1) * TY ? (TX + 2) * TY : (TX + 1) * TY) + 31) / 32 * 32;
+  static constexpr int ctas = 65536 / (threads * 44) > 0 ? 65536 / (threads * 44) : 1;
+};
+
+template <int TX, int TY>
+struct XYSmem {
+  alignas(128) float u[5 * (TY + 4) * (TX + 4)];  // the staged plane (component after component)
+  float fl[5][(TX + 2) * (TY + 2)];               // face states: left / right
+  float fr[5][(TX + 2) * (TY + 2)];
+  float f[5][(TX + 1) * (TY + 1)];                // interface fluxes
+};
+
+template <int TX, int TY>
+__global__ void __launch_bounds__(XYCfg<TX, TY>::threads, XYCfg<TX, TY>::ctas)
+    sweep_xy_kernel(MixedParams M, Geom g, Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
+                    FallbackQueue q, const __grid_constant__ CUtensorMap map, int o_off) {
+  constexpr int NT = XYCfg<TX, TY>::threads;
+  constexpr int PW = TX + 4;               // plane row
+  constexpr int PL = (TX + 4) * (TY + 4);  // plane of one component
+  __shared__ XYSmem<TX, TY> sh;
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ float s_dt[4];  // dt/dx, (0.5 dt)/dx, dt/dy, (0.5 dt)/dy
+  const int NX = g.n[0], NY = g.n[1];
+  const int x0 = blockIdx.x * TX + 1, y0 = blockIdx.y * TY + 1;
+  const int cz = (int)blockIdx.z + 1;
+  const long long F = g.field;
+  float* su = sh.u;
+  if (threadIdx.x == 0) mbar_init(&bar);
+  __syncthreads();
+  // 1. stage the plane: cells x0-2 .. x0+TX+1, y0-2 .. y0+TY+1 of plane cz
+  if (threadIdx.x == 0)
+    tma_load_4d(su, &map, x0 - 1, y0 - 1, cz + 1 + o_off, 0, &bar, (unsigned)(5 * PL * sizeof(float)));
+  if (threadIdx.x == 32) {
+    const float dt = __double2float_rn(*dtp);
+    s_dt[0] = dt * dx.inv_f[0];
+    s_dt[1] = (0.5f * dt) * dx.inv_f[0];
+    s_dt[2] = dt * dx.inv_f[1];
+    s_dt[3] = (0.5f * dt) * dx.inv_f[1];
+  }
+  if (threadIdx.x < 32 && !mbar_wait(&bar, 0)) {
+    if (threadIdx.x == 0) atomicOr(q.status, kStatusTmaTimeout);
+    mbar_wait(&bar, 0);
+  }
+  __syncthreads();
+
+  // an interface the FP32 solve leaves to FP64: queued once (by the tile
+  // whose left face it is, or by the last tile at the box's right boundary)
+  // unless a cell of its stencil is non-finite (then the flux is NaN)
+  auto settle = [&](bool need64, int axis, int li, int T, int N, int ga, long long o, int px, int py,
+                    float* f) {
+    if (!need64) return;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+        finite = finite && isfinite(su[c * PL + (axis == 0 ? py * PW + px + k : (py + k) * PW + px)]);
+    if (finite && (li < T || ga == N)) {
+      const int slot = atomicAdd(q.n, 1);
+      if (slot < q.cap) {
+        FallbackEntry& e = q.e[slot];
+        e.axis = axis;
+        e.ga = ga;
+        e.box = 0;
+        e.o = o + q.o_base;
+      } else {
+        atomicOr(q.status, 2);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) f[c] = finite ? 0.f : __int_as_float(0x7fffffff);
+  };
+
+  // 2. x face states of cells x0-1 .. x0+TX (rows y0 .. y0+TY-1)
+  for (int it = threadIdx.x; it < (TX + 2) * TY; it += NT) {
+    const int la = it % (TX + 2), lb = it / (TX + 2);
+    if (x0 - 1 + la > NX + 1 || y0 + lb > NY) continue;
+    float um[5], u0[5], up[5], l[5], r[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int b = c * PL + (lb + 2) * PW + la;
+      um[c] = su[b];
+      u0[c] = su[b + 1];
+      up[c] = su[b + 2];
+    }
+    face_states<3, 0>(M.G, M.limiter, M.omega, um, u0, up, s_dt[1], l, r);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      sh.fl[c][lb * (TX + 2) + la] = l[c];
+      sh.fr[c][lb * (TX + 2) + la] = r[c];
+    }
+  }
+  __syncthreads();
+  // 3. x interfaces x0-1+li | x0+li
+  for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
+    const int li = it % (TX + 1), lb = it / (TX + 1);
+    if (x0 - 1 + li > NX || y0 + lb > NY) continue;
+    float l[5], r[5], f[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      l[c] = sh.fr[c][lb * (TX + 2) + li];
+      r[c] = sh.fl[c][lb * (TX + 2) + li + 1];
+    }
+    bool need64 = false;
+    rp_flux_f32<3, 0>(M.G, M.rp, l, r, f, &need64);
+    if (!need64) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+        if (!isfinite(f[c])) need64 = true;
+    }
+    const int ga = x0 - 1 + li;
+    settle(need64, 0, li, TX, NX, ga, need64 ? g.at(3, ga, y0 + lb, cz) : 0, li, lb + 2, f);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) sh.f[c][lb * (TX + 1) + li] = f[c];
+  }
+  __syncthreads();
+  // 4. the x flux differences of the tile's cells, held by their threads
+  const int lu = threadIdx.x % TX, lv = threadIdx.x / TX;
+  const bool owner = threadIdx.x < TX * TY && x0 + lu <= NX && y0 + lv <= NY;
+  float ax[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c)
+    ax[c] = owner ? __fmul_rn(s_dt[0], __fsub_rn(sh.f[c][lv * (TX + 1) + lu], sh.f[c][lv * (TX + 1) + lu + 1]))
+                  : 0.f;
+  // 5. y face states of cells y0-1 .. y0+TY (columns x0 .. x0+TX-1)
+  for (int it = threadIdx.x; it < TX * (TY + 2); it += NT) {
+    const int lb = it % TX, la = it / TX;
+    if (y0 - 1 + la > NY + 1 || x0 + lb > NX) continue;
+    float um[5], u0[5], up[5], l[5], r[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int b = c * PL + la * PW + lb + 2;
+      um[c] = su[b];
+      u0[c] = su[b + PW];
+      up[c] = su[b + 2 * PW];
+    }
+    face_states<3, 1>(M.G, M.limiter, M.omega, um, u0, up, s_dt[3], l, r);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      sh.fl[c][la * TX + lb] = l[c];
+      sh.fr[c][la * TX + lb] = r[c];
+    }
+  }
+  __syncthreads();  // also: every thread is done reading the x fluxes
+  // 6. y interfaces y0-1+lj | y0+lj
+  for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
+    const int lb = it % TX, lj = it / TX;
+    if (y0 - 1 + lj > NY || x0 + lb > NX) continue;
+    float l[5], r[5], f[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      l[c] = sh.fr[c][lj * TX + lb];
+      r[c] = sh.fl[c][(lj + 1) * TX + lb];
+    }
+    bool need64 = false;
+    rp_flux_f32<3, 1>(M.G, M.rp, l, r, f, &need64);
+    if (!need64) {
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+        if (!isfinite(f[c])) need64 = true;
+    }
+    const int ga = y0 - 1 + lj;
+    settle(need64, 1, lj, TY, NY, ga, need64 ? g.at(3, x0 + lb, ga, cz) : 0, lb + 2, lj, f);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) sh.f[c][lj * TX + lb] = f[c];
+  }
+  __syncthreads();
+  // 7. acc = dt/dx X + dt/dy Y (the per-axis FIRST and MID roundings)
+  if (owner) {
+    const long long o = g.at(3, x0 + lu, y0 + lv, cz);
+#pragma unroll
+    for (int c = 0; c < 5; ++c)
+      acc[(long long)c * F + o] =
+          __fmaf_rn(s_dt[2], __fsub_rn(sh.f[c][lv * TX + lu], sh.f[c][(lv + 1) * TX + lu]), ax[c]);
+  }
+}
+
 }  // namespace
 }  // namespace rgpu

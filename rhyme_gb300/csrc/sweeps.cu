@@ -158,4 +158,19 @@ cudaError_t RGPU_CAT(launch_batch_sweep_axis_, SWEEP_D)(int axis, int shape, con
   return cudaErrorInvalidValue;
 }
 
+#if SWEEP_D == 3
+cudaError_t launch_sweep_xy_3(const MixedParams& M, const float* Uf, const Geom& g, const Dx& dx,
+                              const double* dtp, float* acc, const FallbackQueue& q, cudaStream_t st) {
+  constexpr int TX = 16, TY = 16;
+  const unsigned gx = (unsigned)((g.n[0] + TX - 1) / TX), gy = (unsigned)((g.n[1] + TY - 1) / TY);
+  if (gy > 65535 || g.n[2] > 65535) return cudaErrorNotSupported;
+  CUtensorMap map;
+  memset(&map, 0, sizeof map);
+  if (!encode_xy_map(&map, Uf, g, TX, TY)) return cudaErrorNotSupported;
+  sweep_xy_kernel<TX, TY><<<dim3(gx, gy, (unsigned)g.n[2]), XYCfg<TX, TY>::threads, 0, st>>>(M, g, dx, dtp, acc, q,
+                                                                                             map, 0);
+  return cudaGetLastError();
+}
+#endif
+
 }  // namespace rgpu
