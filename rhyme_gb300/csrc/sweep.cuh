@@ -163,6 +163,21 @@ struct Axes {
   static constexpr int C = (D == 3) ? 3 - A - B : 2;
 };
 
+// The normal-first component order of axis A in the FP32 face states and
+// interface fluxes: rho, the normal momentum, the other momenta in axis
+// order, E. The FP32 face states and Riemann solve run on vectors in this
+// order (face_states / rp_flux_f32 with axis 0), so every axis executes one
+// copy of their code. nf_comp: the physical component at slot k;
+// nf_slot: the slot of physical component c.
+template <int D, int A>
+__host__ __device__ constexpr int nf_comp(int k) {
+  return (k == 0 || k == D + 1) ? k : (k == 1 ? 1 + A : 1 + ((k - 2) < A ? (k - 2) : (k - 1)));
+}
+template <int D, int A>
+__host__ __device__ constexpr int nf_slot(int c) {
+  return (c == 0 || c == D + 1) ? c : (c == 1 + A ? 1 : 2 + ((c - 1) < A ? (c - 1) : (c - 2)));
+}
+
 // Shared-memory slab; index (la along A, lb along the pencils) is stored
 // with the x-fast index innermost so consecutive threads hit consecutive
 // banks in both orientations. The state slab u is one component plane after
@@ -298,18 +313,20 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     int la, lb;
     split(it, S + 2, la, lb);
     if (a0 - 1 + la > NA + 1 || b0 + lb > NB) continue;
+    // normal-first vectors (nf_comp); the face states stay in that order
     float um[D + 2], u0[D + 2], up[D + 2], l[D + 2], r[D + 2];
 #pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      um[c] = su[c * PLANE + ixu(la, lb)];
-      u0[c] = su[c * PLANE + ixu(la + 1, lb)];
-      up[c] = su[c * PLANE + ixu(la + 2, lb)];
+    for (int k = 0; k < D + 2; ++k) {
+      const int c = nf_comp<D, A>(k);
+      um[k] = su[c * PLANE + ixu(la, lb)];
+      u0[k] = su[c * PLANE + ixu(la + 1, lb)];
+      up[k] = su[c * PLANE + ixu(la + 2, lb)];
     }
-    face_states<D, A>(M.G, limiter, omega, um, u0, up, hdtdx, l, r);
+    face_states<D, 0>(M.G, limiter, omega, um, u0, up, hdtdx, l, r);
 #pragma unroll
-    for (int c = 0; c < D + 2; ++c) {
-      sh.ul[c][ix(la, lb, S + 2)] = l[c];
-      sh.ur[c][ix(la, lb, S + 2)] = r[c];
+    for (int k = 0; k < D + 2; ++k) {
+      sh.ul[k][ix(la, lb, S + 2)] = l[k];
+      sh.ur[k][ix(la, lb, S + 2)] = r[k];
     }
   }
   __syncthreads();
@@ -326,7 +343,7 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
       r[c] = sh.ul[c][ix(li + 1, lb, S + 2)];
     }
     bool need64 = false;
-    rp_flux_f32<D, A>(M.G, M.rp, l, r, f, &need64);
+    rp_flux_f32<D, 0>(M.G, M.rp, l, r, f, &need64);  // normal-first in and out
     if (!need64) {
 #pragma unroll
       for (int c = 0; c < D + 2; ++c)
@@ -382,7 +399,8 @@ __device__ __forceinline__ void sweep_tile(const MixedParams& M, int limiter, fl
     double ud[D + 2];
 #pragma unroll
     for (int c = 0; c < D + 2; ++c)
-      ud[c] = accumulate<MODE>(dtdx, sh.f[c][ix(lu, lb, S + 1)], sh.f[c][ix(lu + 1, lb, S + 1)],
+      ud[c] = accumulate<MODE>(dtdx, sh.f[nf_slot<D, A>(c)][ix(lu, lb, S + 1)],
+                               sh.f[nf_slot<D, A>(c)][ix(lu + 1, lb, S + 1)],
                                PRE_ACC ? pre_acc[c * S * P + it] : 0.f, PRE_U ? pre_u[c * S * P + it] : 0.0,
                                (long long)c * F + o, acc, Unew);
     if (carrying) {
@@ -453,34 +471,40 @@ __global__ void __launch_bounds__(TileCfg<S, P>::threads, TileCfg<S, P>::templat
 // ---- the x and y sweeps of a 3-D box in one kernel ---------------------------
 // A CTA takes a TX x TY tile of one z plane: one TMA copy stages the tile's
 // FP32 state with a 2-cell halo along x and y ((TX+4) x (TY+4) cells, every
-// component), then the x sweep (face states, FP32 interface fluxes, flux
-// differences held in registers) and the y sweep run on it, and the
-// accumulator acc = dt/dx X + dt/dy Y is written once. Every operation is
-// the per-axis sweeps' (FIRST then MID, the same explicit roundings), so
-// the result is bit-identical to sweep_kernel<3,0,...> followed by
-// sweep_kernel<3,1,...>; what it saves is the second staging of the slab
-// and the accumulator's round trip between the two sweeps (40 of the
-// step's 240 bytes per cell). One thread per x interface ((TX+1) TY,
-// rounded up to warps).
+// component); then the face states of both axes (one loop over the x and y
+// items), the interface fluxes of both axes (one loop), and the accumulator
+// acc = dt/dx X + dt/dy Y, written once. The face states and fluxes run on
+// normal-first vectors (nf_comp), so the loops hold one copy of the face
+// state and Riemann code for both axes (two inlined copies cost the kernel
+// as much in instruction-cache misses as the single staging saved). Every
+// operation is the per-axis sweeps' (FIRST then MID, the same roundings):
+// the result is bit-identical to sweep_kernel<3,0,...> then
+// sweep_kernel<3,1,...>; it saves the second staging of the plane and the
+// accumulator's round trip between the two sweeps.
 template <int TX, int TY>
 struct XYCfg {
-  static constexpr int threads = (((TX + 2) * TY > (TX + 1) * TY ? (TX + 2) * TY : (TX + 1) * TY) + 31) / 32 * 32;
+  static constexpr int NXF = (TX + 2) * TY, NYF = TX * (TY + 2);  // face items
+  static constexpr int NXI = (TX + 1) * TY, NYI = TX * (TY + 1);  // interfaces
+  static constexpr int threads = ((NXF > NYF ? NXF : NYF) + 31) / 32 * 32;
   static constexpr int ctas = 65536 / (threads * 44) > 0 ? 65536 / (threads * 44) : 1;
 };
 
 template <int TX, int TY>
 struct XYSmem {
+  static constexpr int NF = XYCfg<TX, TY>::NXF > XYCfg<TX, TY>::NYF ? XYCfg<TX, TY>::NXF : XYCfg<TX, TY>::NYF;
+  static constexpr int NI = XYCfg<TX, TY>::NXI > XYCfg<TX, TY>::NYI ? XYCfg<TX, TY>::NXI : XYCfg<TX, TY>::NYI;
   alignas(128) float u[5 * (TY + 4) * (TX + 4)];  // the staged plane (component after component)
-  float fl[5][(TX + 2) * (TY + 2)];               // face states: left / right
-  float fr[5][(TX + 2) * (TY + 2)];
-  float f[5][(TX + 1) * (TY + 1)];                // interface fluxes
+  float fl[2][5][NF];                             // face states per axis (normal-first): left / right
+  float fr[2][5][NF];
+  float f[2][5][NI];                              // interface fluxes per axis (normal-first)
 };
 
 template <int TX, int TY>
 __global__ void __launch_bounds__(XYCfg<TX, TY>::threads, XYCfg<TX, TY>::ctas)
     sweep_xy_kernel(MixedParams M, Geom g, Dx dx, const double* __restrict__ dtp, float* __restrict__ acc,
                     FallbackQueue q, const __grid_constant__ CUtensorMap map, int o_off) {
-  constexpr int NT = XYCfg<TX, TY>::threads;
+  using Cfg = XYCfg<TX, TY>;
+  constexpr int NT = Cfg::threads;
   constexpr int PW = TX + 4;               // plane row
   constexpr int PL = (TX + 4) * (TY + 4);  // plane of one component
   __shared__ XYSmem<TX, TY> sh;
@@ -509,135 +533,116 @@ __global__ void __launch_bounds__(XYCfg<TX, TY>::threads, XYCfg<TX, TY>::ctas)
   }
   __syncthreads();
 
-  // an interface the FP32 solve leaves to FP64: queued once (by the tile
-  // whose left face it is, or by the last tile at the box's right boundary)
-  // unless a cell of its stencil is non-finite (then the flux is NaN)
-  auto settle = [&](bool need64, int axis, int li, int T, int N, int ga, long long o, int px, int py,
-                    float* f) {
-    if (!need64) return;
-    bool finite = true;
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-#pragma unroll
-      for (int c = 0; c < 5; ++c)
-        finite = finite && isfinite(su[c * PL + (axis == 0 ? py * PW + px + k : (py + k) * PW + px)]);
-    if (finite && (li < T || ga == N)) {
-      const int slot = atomicAdd(q.n, 1);
-      if (slot < q.cap) {
-        FallbackEntry& e = q.e[slot];
-        e.axis = axis;
-        e.ga = ga;
-        e.box = 0;
-        e.o = o + q.o_base;
-      } else {
-        atomicOr(q.status, 2);
-      }
+  // 2. face states: x of cells x0-1 .. x0+TX (rows y0 ..), then y of cells
+  // y0-1 .. y0+TY (columns x0 ..); one loop, the axis only in the indices
+  for (int it = threadIdx.x; it < Cfg::NXF + Cfg::NYF; it += NT) {
+    const int ax = it >= Cfg::NXF;
+    const int t = ax ? it - Cfg::NXF : it;
+    int base, stride, slot;
+    if (!ax) {
+      const int la = t % (TX + 2), lb = t / (TX + 2);
+      if (x0 - 1 + la > NX + 1 || y0 + lb > NY) continue;
+      base = (lb + 2) * PW + la;
+      stride = 1;
+      slot = lb * (TX + 2) + la;
+    } else {
+      const int lb = t % TX, la = t / TX;
+      if (y0 - 1 + la > NY + 1 || x0 + lb > NX) continue;
+      base = la * PW + lb + 2;
+      stride = PW;
+      slot = la * TX + lb;
     }
-#pragma unroll
-    for (int c = 0; c < 5; ++c) f[c] = finite ? 0.f : __int_as_float(0x7fffffff);
-  };
-
-  // 2. x face states of cells x0-1 .. x0+TX (rows y0 .. y0+TY-1)
-  for (int it = threadIdx.x; it < (TX + 2) * TY; it += NT) {
-    const int la = it % (TX + 2), lb = it / (TX + 2);
-    if (x0 - 1 + la > NX + 1 || y0 + lb > NY) continue;
+    const int c1 = ax ? 2 : 1, c2 = ax ? 1 : 2;  // normal-first: the normal momentum first
+    const int comp[5] = {0, c1, c2, 3, 4};
     float um[5], u0[5], up[5], l[5], r[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      const int b = c * PL + (lb + 2) * PW + la;
-      um[c] = su[b];
-      u0[c] = su[b + 1];
-      up[c] = su[b + 2];
+    for (int k = 0; k < 5; ++k) {
+      const int b = comp[k] * PL + base;
+      um[k] = su[b];
+      u0[k] = su[b + stride];
+      up[k] = su[b + 2 * stride];
     }
-    face_states<3, 0>(M.G, M.limiter, M.omega, um, u0, up, s_dt[1], l, r);
+    face_states<3, 0>(M.G, M.limiter, M.omega, um, u0, up, s_dt[ax ? 3 : 1], l, r);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      sh.fl[c][lb * (TX + 2) + la] = l[c];
-      sh.fr[c][lb * (TX + 2) + la] = r[c];
+    for (int k = 0; k < 5; ++k) {
+      sh.fl[ax][k][slot] = l[k];
+      sh.fr[ax][k][slot] = r[k];
     }
   }
   __syncthreads();
-  // 3. x interfaces x0-1+li | x0+li
-  for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
-    const int li = it % (TX + 1), lb = it / (TX + 1);
-    if (x0 - 1 + li > NX || y0 + lb > NY) continue;
+  // 3. interfaces: x0-1+li | x0+li (rows y0 ..), then y0-1+lj | y0+lj
+  for (int it = threadIdx.x; it < Cfg::NXI + Cfg::NYI; it += NT) {
+    const int ax = it >= Cfg::NXI;
+    const int t = ax ? it - Cfg::NXI : it;
+    int li, lb, N, T, ga, px, py, sl, sr, sf;
+    if (!ax) {
+      li = t % (TX + 1);
+      lb = t / (TX + 1);
+      if (x0 - 1 + li > NX || y0 + lb > NY) continue;
+      N = NX, T = TX, ga = x0 - 1 + li, px = li, py = lb + 2;
+      sl = lb * (TX + 2) + li, sr = sl + 1, sf = lb * (TX + 1) + li;
+    } else {
+      lb = t % TX;
+      li = t / TX;
+      if (y0 - 1 + li > NY || x0 + lb > NX) continue;
+      N = NY, T = TY, ga = y0 - 1 + li, px = lb + 2, py = li;
+      sl = li * TX + lb, sr = sl + TX, sf = li * TX + lb;
+    }
     float l[5], r[5], f[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      l[c] = sh.fr[c][lb * (TX + 2) + li];
-      r[c] = sh.fl[c][lb * (TX + 2) + li + 1];
+    for (int k = 0; k < 5; ++k) {
+      l[k] = sh.fr[ax][k][sl];
+      r[k] = sh.fl[ax][k][sr];
     }
     bool need64 = false;
     rp_flux_f32<3, 0>(M.G, M.rp, l, r, f, &need64);
     if (!need64) {
 #pragma unroll
-      for (int c = 0; c < 5; ++c)
-        if (!isfinite(f[c])) need64 = true;
+      for (int k = 0; k < 5; ++k)
+        if (!isfinite(f[k])) need64 = true;
     }
-    const int ga = x0 - 1 + li;
-    settle(need64, 0, li, TX, NX, ga, need64 ? g.at(3, ga, y0 + lb, cz) : 0, li, lb + 2, f);
+    if (need64) {
+      // as the per-axis sweeps: queued once (by the tile whose left face it
+      // is, or by the last tile at the box's right boundary) unless a cell
+      // of its stencil is non-finite (then the flux is NaN)
+      const int step = ax ? PW : 1;
+      bool finite = true;
 #pragma unroll
-    for (int c = 0; c < 5; ++c) sh.f[c][lb * (TX + 1) + li] = f[c];
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) finite = finite && isfinite(su[c * PL + py * PW + px + k * step]);
+      if (finite && (li < T || ga == N)) {
+        const int slot = atomicAdd(q.n, 1);
+        if (slot < q.cap) {
+          FallbackEntry& e = q.e[slot];
+          e.axis = ax;
+          e.ga = ga;
+          e.box = 0;
+          e.o = (ax ? g.at(3, x0 + lb, ga, cz) : g.at(3, ga, y0 + lb, cz)) + q.o_base;
+        } else {
+          atomicOr(q.status, 2);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) f[k] = finite ? 0.f : __int_as_float(0x7fffffff);
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) sh.f[ax][k][sf] = f[k];
   }
   __syncthreads();
-  // 4. the x flux differences of the tile's cells, held by their threads
-  const int lu = threadIdx.x % TX, lv = threadIdx.x / TX;
-  const bool owner = threadIdx.x < TX * TY && x0 + lu <= NX && y0 + lv <= NY;
-  float ax[5];
-#pragma unroll
-  for (int c = 0; c < 5; ++c)
-    ax[c] = owner ? __fmul_rn(s_dt[0], __fsub_rn(sh.f[c][lv * (TX + 1) + lu], sh.f[c][lv * (TX + 1) + lu + 1]))
-                  : 0.f;
-  // 5. y face states of cells y0-1 .. y0+TY (columns x0 .. x0+TX-1)
-  for (int it = threadIdx.x; it < TX * (TY + 2); it += NT) {
-    const int lb = it % TX, la = it / TX;
-    if (y0 - 1 + la > NY + 1 || x0 + lb > NX) continue;
-    float um[5], u0[5], up[5], l[5], r[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      const int b = c * PL + la * PW + lb + 2;
-      um[c] = su[b];
-      u0[c] = su[b + PW];
-      up[c] = su[b + 2 * PW];
-    }
-    face_states<3, 1>(M.G, M.limiter, M.omega, um, u0, up, s_dt[3], l, r);
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      sh.fl[c][la * TX + lb] = l[c];
-      sh.fr[c][la * TX + lb] = r[c];
-    }
-  }
-  __syncthreads();  // also: every thread is done reading the x fluxes
-  // 6. y interfaces y0-1+lj | y0+lj
-  for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
-    const int lb = it % TX, lj = it / TX;
-    if (y0 - 1 + lj > NY || x0 + lb > NX) continue;
-    float l[5], r[5], f[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      l[c] = sh.fr[c][lj * TX + lb];
-      r[c] = sh.fl[c][(lj + 1) * TX + lb];
-    }
-    bool need64 = false;
-    rp_flux_f32<3, 1>(M.G, M.rp, l, r, f, &need64);
-    if (!need64) {
-#pragma unroll
-      for (int c = 0; c < 5; ++c)
-        if (!isfinite(f[c])) need64 = true;
-    }
-    const int ga = y0 - 1 + lj;
-    settle(need64, 1, lj, TY, NY, ga, need64 ? g.at(3, x0 + lb, ga, cz) : 0, lb + 2, lj, f);
-#pragma unroll
-    for (int c = 0; c < 5; ++c) sh.f[c][lj * TX + lb] = f[c];
-  }
-  __syncthreads();
-  // 7. acc = dt/dx X + dt/dy Y (the per-axis FIRST and MID roundings)
-  if (owner) {
+  // 4. acc = dt/dx X + dt/dy Y (the per-axis FIRST and MID roundings); the
+  // y fluxes hold m_y in slot 1 and m_x in slot 2
+  for (int it = threadIdx.x; it < TX * TY; it += NT) {
+    const int lu = it % TX, lv = it / TX;
+    if (x0 + lu > NX || y0 + lv > NY) continue;
     const long long o = g.at(3, x0 + lu, y0 + lv, cz);
 #pragma unroll
-    for (int c = 0; c < 5; ++c)
+    for (int c = 0; c < 5; ++c) {
+      const int ky = (c == 1) ? 2 : (c == 2 ? 1 : c);
+      const float ax_ = __fmul_rn(s_dt[0], __fsub_rn(sh.f[0][c][lv * (TX + 1) + lu], sh.f[0][c][lv * (TX + 1) + lu + 1]));
       acc[(long long)c * F + o] =
-          __fmaf_rn(s_dt[2], __fsub_rn(sh.f[c][lv * TX + lu], sh.f[c][(lv + 1) * TX + lu]), ax[c]);
+          __fmaf_rn(s_dt[2], __fsub_rn(sh.f[1][ky][lv * TX + lu], sh.f[1][ky][(lv + 1) * TX + lu]), ax_);
+    }
   }
 }
 
