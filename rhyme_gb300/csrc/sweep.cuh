@@ -9,7 +9,8 @@
 // Riemann problems of the slab in FP32 (one thread per interface) and forms
 // the flux difference of its S cells. The tile shape (S, P) is a template
 // parameter; sweeps.cu instantiates every shape of the candidate set for
-// the autotuner, once per dimensionality.
+// the autotuner, once per dimensionality. sweep_xy_kernel (end of the file)
+// runs the x and y sweeps of a 3-D box in one kernel.
 #pragma once
 
 #include <cuda.h>
@@ -189,9 +190,9 @@ __host__ __device__ constexpr int nf_slot(int c) {
 template <int D, int S, int P>
 struct SweepSmem {
   alignas(128) float u[(D + 2) * (S + 4) * (P + 4)];  // FP32 state slab (ghost/halo layer included)
-  float ul[D + 2][(S + 2) * P];  // face states, left / right
+  float ul[D + 2][(S + 2) * P];  // face states (normal-first), left / right
   float ur[D + 2][(S + 2) * P];
-  float f[D + 2][(S + 1) * P];   // interface fluxes
+  float f[D + 2][(S + 1) * P];   // interface fluxes (normal-first)
 };
 
 // One slab (tile tA along the sweep axis, tB across the pencils, plane cC)
