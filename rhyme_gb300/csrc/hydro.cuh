@@ -343,13 +343,6 @@ __device__ __forceinline__ T guess_p_star_adaptive(const Gas<T>& G, T l_rho, T v
   return p;
 }
 
-// Guess 0, floored at tiny, inlined (the mixed form's FP32 solve).
-template <typename T>
-__device__ __forceinline__ T guess_p_star_first(const Gas<T>& G, T l_rho, T vl, T l_p, T l_cs, T r_rho, T vr,
-                                                T r_p, T r_cs) {
-  return fmax_ref(guess_p_star_adaptive(G, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs), Limits<T>::tiny());
-}
-
 // Guess number k (0..5) of rhyme_irs_guess_p_star.f90:14-71, floored at tiny.
 template <typename T>
 __device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T l_p, T l_cs, T r_rho,
@@ -377,15 +370,11 @@ __device__ __noinline__ T guess_p_star(const Gas<T>& G, int k, T l_rho, T vl, T 
 }
 
 // rhyme_irs_exec.f90:19-44 with lazily evaluated guesses. l_f / r_f are the
-// wave functions at the last iterate before the final update. `converged`
-// (optional) tells whether the first guess met the tolerance within the
-// iteration cap.
+// wave functions at the last iterate before the final update.
 template <typename T, bool LAZY>
 __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
-                                      T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f,
-                                      bool* converged = nullptr) {
+                                      T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f) {
   T p_star = T(0), p_prev, l_fp, r_fp;
-  if (converged) *converged = false;
   WaveSide<T> WL = wave_side<T, LAZY>(G, l_rho, l_p, l_cs);
   WaveSide<T> WR = wave_side<T, LAZY>(G, r_rho, r_p, r_cs);
   for (int gid = 0; gid < 6; ++gid) {
@@ -396,42 +385,10 @@ __device__ __forceinline__ T irs_exec(const Gas<T>& G, T tol, int n_iter, T l_rh
       nonlinear_wave<T, LAZY>(G, WR, p_star, r_f, r_fp);
       p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
       if (p_star < T(0)) break;
-      if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) {
-        if (converged && gid == 0) *converged = true;
-        break;
-      }
+      if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) break;
       p_prev = p_star;
     }
     if (p_star > T(0)) break;
-  }
-  if (p_star < T(0)) p_star = T(0);
-  return p_star;
-}
-
-// The first guess's Newton iteration alone (the mixed form's FP32 solve):
-// the same operations as irs_exec's first pass, inlined, with the later
-// guesses left out. An interface whose first guess does not meet the
-// tolerance is redone in FP64 (rp_solve with CHECK), so this returns the
-// same p* as irs_exec wherever its result is used.
-template <typename T>
-__device__ __forceinline__ T irs_exec_first(const Gas<T>& G, T tol, int n_iter, T l_rho, T vl, T l_p, T l_cs,
-                                            T& l_f, T r_rho, T vr, T r_p, T r_cs, T& r_f, bool* converged) {
-  T l_fp, r_fp;
-  *converged = false;
-  WaveSide<T> WL = wave_side<T, false>(G, l_rho, l_p, l_cs);
-  WaveSide<T> WR = wave_side<T, false>(G, r_rho, r_p, r_cs);
-  T p_star = guess_p_star_first(G, l_rho, vl, l_p, l_cs, r_rho, vr, r_p, r_cs);
-  T p_prev = p_star;
-  for (int i = 1; i <= n_iter; ++i) {
-    nonlinear_wave<T, false>(G, WL, p_star, l_f, l_fp);
-    nonlinear_wave<T, false>(G, WR, p_star, r_f, r_fp);
-    p_star = p_prev - (l_f + r_f + (vr - vl)) / (l_fp + r_fp);
-    if (p_star < T(0)) break;
-    if (T(2) * m_abs(p_star - p_prev) / (p_star + p_prev) < tol) {
-      *converged = true;
-      break;
-    }
-    p_prev = p_star;
   }
   if (p_star < T(0)) p_star = T(0);
   return p_star;
@@ -451,22 +408,17 @@ struct Star {
   T l_rho, l_speed, l_cs, l_speedH, l_speedT;  // speed = shock speed
   T r_rho, r_speed, r_cs, r_speedH, r_speedT;
   T l_f, r_f;
-  bool converged;  // first guess met the tolerance
 };
 
 // rhyme_riemann_problem_star.f90:12-65, split so that only the side the
 // sampling reads is formed: p* and u* (:12-38), then the left (:40, 43-53)
 // or the right (:41, 55-65) star state, each with the reference's
 // operations.
-template <int D, int AX, typename T, bool LAZY, bool FIRST_ONLY = false>
+template <int D, int AX, typename T, bool LAZY>
 __device__ __forceinline__ void rp_star_pu(const Gas<T>& G, const Rp<T>& rp, const Side<D, T>& L,
                                            const Side<D, T>& R, Star<T>& s) {
-  if constexpr (FIRST_ONLY)
-    s.p = irs_exec_first<T>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
-                            s.r_f, &s.converged);
-  else
-    s.p = irs_exec<T, LAZY>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
-                            s.r_f, &s.converged);
+  s.p = irs_exec<T, LAZY>(G, rp.tol, rp.n_iter, L.rho, L.v[AX], L.p, L.cs, s.l_f, R.rho, R.v[AX], R.p, R.cs,
+                          s.r_f);
   if (s.p < rp.vac_p) s.p = rp.vac_p;
   s.u = T(0.5) * ((R.v[AX] + L.v[AX]) + (s.r_f - s.l_f));
 }
@@ -597,14 +549,12 @@ __device__ __forceinline__ void vacuum_state(const Gas<T>& G, const Rp<T>& rp, T
   prim_vars_to_cons<D>(G, rp.vac_rho, v, rp.vac_p, u);
 }
 
-// rhyme_riemann_problem_solve.f90:17-103 sampled at x/t = dxdt.
-// With CHECK, *need64 is set when the interface should be redone in double:
-// a vacuum or vacuum-generation branch, an interface within 10% of vacuum
-// generation or with a density or pressure ratio beyond 1e6, a first guess
-// whose Newton iteration missed the tolerance, or a non-finite state.
-template <int D, int AX, typename T, bool CHECK = false, bool LAZY = false>
+// rhyme_riemann_problem_solve.f90:17-103 sampled at x/t = dxdt. (The mixed
+// sweeps' FP32 interfaces go through rp_flux_f32 instead, which sends the
+// interfaces this solver handles in its vacuum branches to the FP64 one.)
+template <int D, int AX, typename T, bool LAZY = false>
 __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
-                                         T dxdt, T* u, bool* need64 = nullptr) {
+                                         T dxdt, T* u) {
   Side<D, T> L, R;
   L.rho = fmax_ref(l[0], rp.vac_rho);
   R.rho = fmax_ref(r[0], rp.vac_rho);
@@ -613,10 +563,6 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
   const bool vacuum_left = L.rho < e_rho && R.rho > e_rho;
   const bool vacuum_both = L.rho < e_rho && R.rho < e_rho;
   const T tiny = Limits<T>::tiny();
-  if (CHECK && (vacuum_right || vacuum_left || vacuum_both)) {
-    *need64 = true;
-    return;
-  }
 
   if (vacuum_right) {
 #pragma unroll
@@ -656,14 +602,6 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
     R.cs = fmax_ref(sound_speed<D>(G, r), tiny);
     T du = R.v[AX] - L.v[AX];
     T du_crit = T(2) * (L.cs + R.cs) / G.gm1;
-    if (CHECK) {
-      const T rmin = fmin_ref(L.rho, R.rho), rmax = fmax_ref(L.rho, R.rho);
-      const T pmin = fmin_ref(L.p, R.p), pmax = fmax_ref(L.p, R.p);
-      if (!(du_crit - du > T(0.1) * du_crit) || !(rmin * T(1e6) > rmax) || !(pmin * T(1e6) > pmax)) {
-        *need64 = true;
-        return;
-      }
-    }
     if (du_crit < du) {  // vacuum generation
       const T s_starl = L.v[AX] - T(2) * L.cs / G.gm1;
       const T s_starr = R.v[AX] + T(2) * R.cs / G.gm1;
@@ -680,13 +618,7 @@ __device__ __forceinline__ void rp_solve(const Gas<T>& G, const Rp<T>& rp, const
       }
     } else {
       Star<T> s;
-      // with CHECK, an interface whose first guess misses is redone in FP64:
-      // the later guesses are never used
-      rp_star_pu<D, AX, T, LAZY, CHECK>(G, rp, L, R, s);
-      if (CHECK && !s.converged) {
-        *need64 = true;
-        return;
-      }
+      rp_star_pu<D, AX, T, LAZY>(G, rp, L, R, s);
       rp_sampling<D, AX>(G, L, R, l, r, s, dxdt, u);
     }
   }
@@ -865,7 +797,7 @@ template <int D, int AX, typename T, bool LAZY = false>
 __device__ __forceinline__ void interface_flux(const Gas<T>& G, const Rp<T>& rp, const T* l, const T* r,
                                                T* f) {
   T u[D + 2];
-  rp_solve<D, AX, T, false, LAZY>(G, rp, l, r, T(0), u);
+  rp_solve<D, AX, T, LAZY>(G, rp, l, r, T(0), u);
   flux<D, AX>(G, u, f);
 }
 
